@@ -1,0 +1,321 @@
+"""Benchmark of the focal-stencil hot path on GB300.
+
+Default workload: fused slope + aspect + hillshade (azimuth 315, altitude 45)
+over one 16384 x 16384 float32 fBm DEM (0-4500 m, 10 m cells, -9999 in 200
+disc holes).  A step is one fused pass over the whole DEM.  Inputs (1 GiB)
+and outputs (2.25 GiB) are far larger than the 129 MB L2, so no flush is
+needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl vsr|reference]
+
+Prints ONE JSON line (rank 0).  ``value`` is device throughput (Gpixel/s) with
+the DEM resident in HBM; ``e2e`` is the same metric through the public API
+(from_numpy of a pinned host DEM -> raster_terrain -> to_numpy into pinned
+host buffers), copies included.  ``--impl reference`` times the reference's
+CPU algorithm (the float64 numpy restatement in oracle/, the reference being
+pure Python) on the host cores.  Under torchrun each rank runs its own
+replica (the path shards by raster; no collective on the data path).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+for _p in (str(ROOT), str(ROOT / "vibespatial-raster_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "Gpixel/s & % roofline: slope/aspect, conv; batched/split-BF16 vs plain FP32"
+UNIT = "Gpixel/s"
+BYTES_PER_PX = 13  # read f32 DEM 4 + slope 4 + aspect 4 + hillshade 1
+WORKLOAD = "fused slope+aspect+hillshade, 16384x16384 f32 fBm DEM, 10 m cells, 200 -9999 disc holes"
+
+
+def _dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle sampler running during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _roofline_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------- CPU legs --
+def _oracle_terrain_strip(dem: np.ndarray, y0: int, y1: int, affine, nodata):
+    """Reference CPU path (slope, aspect, hillshade: three calls) on rows [y0, y1)."""
+    import oracle
+
+    lo, hi = max(0, y0 - 1), min(dem.shape[0], y1 + 1)
+    strip = dem[lo:hi]
+    s, _ = oracle.slope_aspect(strip, affine, nodata, compute_slope=True, compute_aspect=False)
+    _, a = oracle.slope_aspect(strip, affine, nodata, compute_slope=False, compute_aspect=True)
+    h, _ = oracle.hillshade(strip, affine, nodata)
+    return s.astype(np.float32), a.astype(np.float32), h
+
+
+def cpu_sample(dem_host: np.ndarray, affine, nodata, rows: int, threads: int):
+    """Time the oracle over ``rows`` rows split into strips over ``threads`` threads."""
+    H = dem_host.shape[0]
+    y0 = (H - rows) // 2
+    strips = max(1, threads)
+    step = (rows + strips - 1) // strips
+    spans = [(y0 + i * step, min(y0 + rows, y0 + (i + 1) * step)) for i in range(strips)]
+    t0 = time.perf_counter()
+    if threads <= 1:
+        for a, b in spans:
+            _oracle_terrain_strip(dem_host, a, b, affine, nodata)
+    else:
+        with ThreadPoolExecutor(max_workers=threads) as ex:
+            list(ex.map(lambda s: _oracle_terrain_strip(dem_host, s[0], s[1], affine, nodata), spans))
+    dt = time.perf_counter() - t0
+    return rows * dem_host.shape[1], dt
+
+
+def run_reference(args, ws, rank):
+    """--impl reference: the reference CPU algorithm on all host cores."""
+    if rank != 0:
+        return
+    import torch
+
+    from vsr_gb300 import workloads
+
+    dem = workloads.terrain_16k(device="cuda" if torch.cuda.is_available() else "cpu")
+    host = dem.data.cpu().numpy()
+    cores = len(os.sched_getaffinity(0))
+    rows = 1024
+    for _ in range(args.warmup):
+        cpu_sample(host, dem.affine, dem.nodata, rows, cores)
+    times = []
+    px = 0
+    for _ in range(args.steps):
+        n, dt = cpu_sample(host, dem.affine, dem.nodata, rows, cores)
+        times.append(dt)
+        px += n
+    total = sum(times)
+    value = px / total / 1e9
+    sample = f"{rows} rows x 16384 of the DEM per step, split into {cores} row strips (1-row halo) over {cores} threads"
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "cpu_path": "reference float64 numpy algorithm (oracle port: slope, aspect, hillshade as 3 calls)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------- GPU leg --
+def run_vsr(args, ws, rank, local):
+    import torch
+
+    import vsr_gb300 as vsr
+    from vsr_gb300 import algebra, workloads
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    vsr.load_library()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    dem = workloads.terrain_16k(device=dev)
+    H, W = dem.data.shape
+    px = H * W
+    r = vsr.from_device(dem.data, nodata=dem.nodata, affine=dem.affine)
+    outs = (torch.empty((1, H, W), dtype=torch.float32, device=dev),
+            torch.empty((1, H, W), dtype=torch.float32, device=dev),
+            torch.empty((1, H, W), dtype=torch.uint8, device=dev))
+
+    def step():
+        algebra.horn_fused(r, out=outs)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    ms = e0.elapsed_time(e1)
+    # per-launch duration of the dominant kernel (one launch per step)
+    launch_ms = []
+    for _ in range(5):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        step()
+        b.record(stream)
+        b.synchronize()
+        launch_ms.append(a.elapsed_time(b))
+
+    # ---- end-to-end through the public API with host buffers ----
+    host_in = torch.empty((H, W), dtype=torch.float32, pin_memory=True)
+    host_in.copy_(dem.data)
+    host_out = [torch.empty((H, W), dtype=torch.float32, pin_memory=True),
+                torch.empty((H, W), dtype=torch.float32, pin_memory=True),
+                torch.empty((H, W), dtype=torch.uint8, pin_memory=True)]
+    in_np = host_in.numpy()
+    out_np = [t.numpy() for t in host_out]
+
+    def e2e_step():
+        rr = vsr.from_numpy(in_np, nodata=dem.nodata, affine=dem.affine)
+        res = vsr.raster_terrain(rr)
+        res["slope"].to_numpy(out=out_np[0])
+        res["aspect"].to_numpy(out=out_np[1])
+        res["hillshade"].to_numpy(out=out_np[2])
+
+    e2e_step()
+    torch.cuda.synchronize()
+    e2e_steps = max(3, min(args.steps, 10))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    clocks = sampler.stop()
+
+    # max over ranks
+    t_step = ms / args.steps
+    if ws > 1:
+        tt = torch.tensor([t_step, e2e_s], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_step, e2e_s = float(tt[0]), float(tt[1])
+    value = ws * px / (t_step * 1e-3) / 1e9
+    e2e_value = ws * px / e2e_s / 1e9
+
+    if rank == 0:
+        peak, peak_kind = _roofline_peak()
+        lmed = statistics.median(launch_ms)
+        achieved = BYTES_PER_PX * px / (lmed * 1e-3) / 1e9
+        traffic_file = ROOT / "profiles" / "horn_f32_tma_terrain16k_traffic.json"
+        traffic = None
+        if traffic_file.exists():
+            traffic = json.loads(traffic_file.read_text()).get("bytes_per_launch")
+        # CPU baseline: the oracle, single thread, on a bounded row sample.
+        host = in_np
+        cpu_rows = 512
+        n, dt = cpu_sample(host, dem.affine, dem.nodata, cpu_rows, 1)
+        n2, dt2 = cpu_sample(host, dem.affine, dem.nodata, cpu_rows, 1)
+        cpu_val = (n + n2) / (dt + dt2) / 1e9
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "pixels": px, "bytes_per_pixel": BYTES_PER_PX,
+                       "l2": "inputs+outputs (3.5 GB/step) exceed L2; no flush",
+                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+            "gpu_launches": args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                         "kernel": "horn_f32_tma", "launch_ms": lmed},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": px * 4,
+                    "d2h_bytes_per_step": px * 9, "ms_per_step": e2e_s * 1e3},
+            "cpu_baseline": {"value": cpu_val, "unit": UNIT, "cores": 1, "kind": "port",
+                             "sample": f"2 x {cpu_rows} rows x {W} px (1-row halo) of the same DEM, reference "
+                                       "float64 numpy algorithm, 3 calls (slope, aspect, hillshade), 1 thread"},
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["vsr", "reference"], default="vsr")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    ws, rank, local = _dist_env()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_vsr(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

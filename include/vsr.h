@@ -1,0 +1,164 @@
+/*
+ * vsr.h -- C ABI of libvsr, the GB300 (sm_103a) focal-stencil library that
+ * replaces vibespatial-raster's per-op NVRTC kernels and CuPy launch glue.
+ *
+ * The reference's operator boundary is its runtime launcher:
+ *   get_cuda_runtime().compile_kernels(...) / .launch(kernel=, grid=, block=,
+ *   params=(values, types), shared_mem_bytes=)
+ * called from src/vibespatial/raster/algebra.py with raw device pointers
+ * (CuPy ``.data.ptr``), a nullable uint8 nodata mask, int32 sizes and
+ * float64 scalars.  Each entry point below replaces one such launch (plus the
+ * float64 up-cast, mask materialisation and down-cast passes around it) and
+ * cites the launch it replaces.
+ *
+ * Conventions
+ *   - Every function returns an int status (VSR_OK == 0) and never throws;
+ *     vsr_last_error() gives a message for the calling thread.
+ *   - The caller owns every buffer.  Pointers are device pointers unless the
+ *     parameter name ends in _host.  Pitches are in elements.
+ *   - Work is enqueued on ``stream`` (a cudaStream_t, NULL = legacy default
+ *     stream) and the call returns without waiting for it, except where a
+ *     function says otherwise.
+ *   - Distinct streams may be driven from distinct host threads.
+ */
+#ifndef VSR_H_
+#define VSR_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define VSR_API __attribute__((visibility("default")))
+#else
+#define VSR_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define VSR_OK 0
+#define VSR_ERR_INVALID_ARG 1  /* bad size, pointer, dtype or parameter     */
+#define VSR_ERR_UNSUPPORTED 2  /* valid request this build does not serve  */
+#define VSR_ERR_CUDA 3         /* a CUDA runtime/driver call failed         */
+#define VSR_ERR_WORKSPACE 4    /* workspace NULL, misaligned or too small   */
+#define VSR_ERR_DEVICE 5       /* a kernel reported a device-side error     */
+
+/* ---- element types ----------------------------------------------------- */
+#define VSR_U8 1
+#define VSR_I16 2
+#define VSR_U16 3
+#define VSR_I32 4
+#define VSR_F32 5
+#define VSR_F64 6
+
+/* ---- nodata kinds ------------------------------------------------------ */
+#define VSR_NODATA_NONE 0  /* raster has no nodata value                    */
+#define VSR_NODATA_VALUE 1 /* pixel == nodata (compared exactly, as float64) */
+#define VSR_NODATA_NAN 2   /* pixel is NaN                                  */
+
+/* ---- Horn flags -------------------------------------------------------- */
+/* Slope/aspect nodata only at the centre pixel, neighbours' raw values used
+ * (the reference GPU kernel, kernels/focal.py:245-262).  Default (flag clear)
+ * is the reference CPU rule: any pixel whose 3x3 window touches nodata
+ * (algebra.py:2218-2247). */
+#define VSR_HORN_CENTER_ONLY 1u
+/* Slope/aspect do not mask NaN nodata; NaN propagates through the gradient
+ * instead.  This is the reference CPU behaviour (its mask is data == NaN,
+ * algebra.py:2188-2189).  Hillshade always masks. */
+#define VSR_HORN_SA_NAN_UNMASKED 2u
+
+/* ---- precision for focal convolution ----------------------------------- */
+#define VSR_PREC_AUTO 0       /* split-BF16 tensor cores for k >= 15, else FP32 */
+#define VSR_PREC_FP32 1       /* FP32 CUDA-core direct / separable kernels      */
+#define VSR_PREC_SPLIT_BF16 2 /* tcgen05 implicit GEMM, hi/lo BF16, FP32 accum  */
+
+/* ---- library ------------------------------------------------------------ */
+VSR_API int vsr_version(void);                 /* major*10000 + minor*100 + patch      */
+VSR_API const char* vsr_last_error(void);      /* message of this thread's last error  */
+/* SM count and compute capability of the current device (cudaGetDevice). */
+VSR_API int vsr_device_info(int* sm_count, int* cc_major, int* cc_minor);
+/* Synchronise ``stream``, then read and clear the device-side error word that
+ * kernels set when a bounded wait ran out (0 = none).  Synchronises. */
+VSR_API int vsr_poll_device_error(void* stream, uint32_t* code);
+
+/* ---- Horn 3x3: slope / aspect / hillshade in one pass -------------------
+ * Replaces the launches of ``slope_aspect`` (algebra.py:2372-2377, kernel
+ * kernels/focal.py:173-283) and ``hillshade`` (algebra.py:2748-2754, kernel
+ * kernels/focal.py:303-467), plus the float64 up-cast (algebra.py:2283,
+ * 2670-2671), the uint8 mask pass (algebra.py:2296-2302, 2687-2696) and the
+ * down-cast (algebra.py:2426-2427).  Edge-replicated borders.
+ *
+ * dem          : height x width raster of ``dtype`` with row pitch ``pitch``
+ * cell_x/_y    : |affine a| and |affine e| (1.0 where zero), float64
+ * nodata/kind  : nodata value and VSR_NODATA_* kind
+ * flags        : VSR_HORN_* bits
+ * slope/aspect : outputs in degrees of ``out_dtype`` (VSR_F32 or VSR_F64),
+ *                row pitch ``out_pitch``; either may be NULL to skip it.
+ *                Nodata pixels receive ``nodata``.
+ * hillshade    : uint8 output (row pitch ``hs_pitch``) or NULL; nodata -> 0.
+ * z_factor, zenith_rad, azimuth_rad : hillshade parameters; the reference
+ *                converts altitude/azimuth degrees to these radians on the
+ *                host (algebra.py:2683-2684).
+ */
+VSR_API int vsr_horn_fused(const void* dem, int dtype, int64_t height, int64_t width, int64_t pitch,
+                   double cell_x, double cell_y, double nodata, int nodata_kind, uint32_t flags,
+                   void* slope, void* aspect, int out_dtype, int64_t out_pitch,
+                   uint8_t* hillshade, int64_t hs_pitch, double z_factor, double zenith_rad,
+                   double azimuth_rad, void* stream);
+
+/* ---- nodata-aware normalised focal convolution --------------------------
+ * Replaces the ``convolve_normalized`` launch (algebra.py:2077-2083, kernel
+ * kernels/focal.py:36-146) with its up-cast, mask and weight-copy passes
+ * (algebra.py:1990-2013).  out[y,x] = sum w*v*valid / sum w*valid over the
+ * in-bounds taps of the kh x kw window centred at (kh/2, kw/2), correlation
+ * orientation; nodata centre or weight sum <= 0 -> ``nodata`` (pass 0.0 when
+ * the raster has none).  A NaN anywhere in the window gives NaN, as in the
+ * reference (NaN * 0 = NaN there).
+ *
+ * weights_host : kh*kw float64 row-major weights in HOST memory
+ * precision    : VSR_PREC_*
+ * workspace    : device scratch of vsr_convolve_workspace_size() bytes,
+ *                256-byte aligned.  The host weights are copied into it with
+ *                cudaMemcpyAsync on ``stream`` (so the call returns after the
+ *                host copy has been staged) and turned into the kernel's
+ *                operand images there by a small float64 prep kernel.
+ */
+VSR_API size_t vsr_convolve_workspace_size(int kh, int kw, int precision);
+VSR_API int vsr_convolve(const void* src, int dtype, int64_t height, int64_t width, int64_t pitch,
+                 const double* weights_host, int kh, int kw, double nodata, int nodata_kind,
+                 void* dst, int out_dtype, int64_t out_pitch, int precision, void* workspace,
+                 size_t workspace_bytes, void* stream);
+
+/* ---- Gaussian filter -----------------------------------------------------
+ * Replaces raster_gaussian_filter (algebra.py:2120-2154): weights built in
+ * float64 on the device (g_i = exp(-0.5 (i - k/2)^2 / sigma^2)); the filter is
+ * evaluated separably (row pass held in shared memory, then the column pass),
+ * which equals the reference's dense k x k normalised correlation with
+ * weights outer(g, g) / sum exactly in real arithmetic, nodata and borders
+ * included.  kernel_size <= 0 selects the default 2*ceil(3 sigma)+1; even
+ * sizes are bumped to odd.  Same output rule as vsr_convolve.
+ */
+VSR_API size_t vsr_gaussian_workspace_size(int kernel_size, int precision);
+VSR_API int vsr_gaussian(const void* src, int dtype, int64_t height, int64_t width, int64_t pitch,
+                 double sigma, int kernel_size, double nodata, int nodata_kind, void* dst,
+                 int out_dtype, int64_t out_pitch, int precision, void* workspace,
+                 size_t workspace_bytes, void* stream);
+
+/* ---- focal mean ----------------------------------------------------------
+ * Replaces the ``focal_stats`` launch with stat_type 2 (algebra.py:3239-3349,
+ * kernel kernels/focal.py:672-769) and the CPU ``_focal_mean_cpu``
+ * (algebra.py:3083-3101): mean of the in-bounds, non-nodata, non-NaN values
+ * of the (2ry+1) x (2rx+1) window; a nodata centre or an empty window gives
+ * ``nodata`` (0.0 when none).  Integer inputs are summed exactly.
+ */
+VSR_API int vsr_focal_mean(const void* src, int dtype, int64_t height, int64_t width, int64_t pitch,
+                   int radius_y, int radius_x, double nodata, int nodata_kind, void* dst,
+                   int out_dtype, int64_t out_pitch, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VSR_H_ */

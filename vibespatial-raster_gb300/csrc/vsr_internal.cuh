@@ -1,0 +1,156 @@
+// Internal helpers shared by the libvsr translation units: error reporting,
+// element-type traits, nodata tests, mbarrier / TMA wrappers with bounded
+// waits, and tensor-map encoding through the driver entry point.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cmath>
+#include <cstdio>
+#include <string>
+
+#include "vsr.h"
+
+namespace vsr {
+
+// ---------------------------------------------------------------- errors --
+void set_error(const char* fmt, ...);
+int fail(int code, const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define VSR_CUDA_TRY(expr)                                   \
+  do {                                                       \
+    cudaError_t _e = (expr);                                 \
+    if (_e != cudaSuccess) return ::vsr::cuda_fail(_e, #expr); \
+  } while (0)
+
+// Device-side error word.  Kernels OR a code into it when a bounded wait
+// runs out; the host reads it with vsr_poll_device_error.  The word is a
+// file-scope __device__ variable of vsr_api.cu; kernels receive its device
+// address (device_error_word(), resolved once per device) as a parameter.
+enum DeviceError : uint32_t {
+  kDevErrTmaTimeout = 1u,
+  kDevErrMmaTimeout = 2u,
+  kDevErrQueue = 4u,
+};
+uint32_t* device_error_word();  // nullptr (and error set) on failure
+
+// Wall-clock bound for every spin-wait in a kernel (nanoseconds).
+constexpr uint64_t kWaitLimitNs = 2000000000ull;
+
+int sm_count();  // cached per device
+
+// ----------------------------------------------------------- dtype traits --
+inline size_t dtype_size(int dt) {
+  switch (dt) {
+    case VSR_U8: return 1;
+    case VSR_I16:
+    case VSR_U16: return 2;
+    case VSR_I32:
+    case VSR_F32: return 4;
+    case VSR_F64: return 8;
+    default: return 0;
+  }
+}
+
+// Decide how a nodata value is tested in the element type itself.  A value
+// that the element type cannot hold exactly never matches any pixel (the
+// reference compares the float64 up-cast against float(nodata)), so the
+// kind degrades to NONE.  Returns the kind to use.
+int resolve_nodata(int dtype, double nodata, int kind, double* as_elem);
+
+template <typename T>
+struct NodataTest {
+  int kind;  // VSR_NODATA_*
+  T value;
+  __device__ __forceinline__ bool operator()(T v) const {
+    if (kind == VSR_NODATA_VALUE) return v == value;
+    if (kind == VSR_NODATA_NAN) return v != v;  // only floats reach here
+    return false;
+  }
+};
+
+// ------------------------------------------------------- device helpers --
+__device__ __forceinline__ uint64_t global_timer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait on an mbarrier phase.  Returns false (and ORs ``code`` into
+// *err_word) if the phase did not complete within kWaitLimitNs.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
+                                                  uint32_t* err_word, uint32_t code) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_timer_ns();
+  while (!mbar_try_wait(bar, parity)) {
+    if (global_timer_ns() - t0 > kWaitLimitNs) {
+      atomicOr(err_word, code);
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// 2-D tiled TMA load of box (x, y) into shared memory, completing on ``bar``.
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void prefetch_tensormap(const CUtensorMap* map) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+
+// ------------------------------------------------------------ host side --
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// dependency on libcuda).
+int encode_tensor_map_2d(CUtensorMap* map, CUtensorMapDataType type, size_t elem_bytes,
+                         const void* base, uint64_t width, uint64_t height, uint64_t pitch_elems,
+                         uint32_t box_w, uint32_t box_h);
+
+inline bool aligned(const void* p, size_t a) {
+  return (reinterpret_cast<uintptr_t>(p) % a) == 0;
+}
+
+}  // namespace vsr

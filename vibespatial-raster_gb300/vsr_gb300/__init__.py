@@ -1,0 +1,42 @@
+"""vsr_gb300 -- GB300-native focal stencils behind vibespatial-raster's API.
+
+Public names mirror ``vibespatial.raster`` for the focal path
+(src/vibespatial/raster/__init__.py:143-187 resolves them lazily there).
+"""
+
+from __future__ import annotations
+
+__version__ = "0.1.0"
+
+from vsr_gb300._lib import load as load_library  # noqa: F401
+from vsr_gb300.algebra import (  # noqa: F401
+    raster_aspect,
+    raster_hillshade,
+    raster_slope,
+    raster_terrain,
+)
+from vsr_gb300.buffers import (  # noqa: F401
+    OwnedRasterArray,
+    RasterDeviceState,
+    RasterDiagnosticEvent,
+    RasterDiagnosticKind,
+    from_device,
+    from_numpy,
+)
+from vsr_gb300.residency import Residency, TransferTrigger  # noqa: F401
+
+__all__ = [
+    "OwnedRasterArray",
+    "RasterDeviceState",
+    "RasterDiagnosticEvent",
+    "RasterDiagnosticKind",
+    "Residency",
+    "TransferTrigger",
+    "from_device",
+    "from_numpy",
+    "load_library",
+    "raster_aspect",
+    "raster_hillshade",
+    "raster_slope",
+    "raster_terrain",
+]

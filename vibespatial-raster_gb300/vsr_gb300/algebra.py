@@ -1,0 +1,267 @@
+"""Focal-stencil operations on OwnedRasterArray, backed by libvsr (sm_103a).
+
+Drop-in counterparts of the reference's public functions in
+src/vibespatial/raster/algebra.py -- same names, arguments, dtype rules,
+nodata conventions, diagnostics prefixes and errors:
+
+=====================  ==============================  ==========================
+function               reference                        libvsr entry point
+=====================  ==============================  ==========================
+raster_slope           algebra.py:2386-2459             vsr_horn_fused
+raster_aspect          algebra.py:2462-2535             vsr_horn_fused
+raster_hillshade       algebra.py:2778-2818             vsr_horn_fused
+raster_convolve        algebra.py:2101-2117             vsr_convolve
+raster_gaussian_filter algebra.py:2120-2154             vsr_gaussian
+raster_focal_mean      algebra.py:3582-3604             vsr_focal_mean
+=====================  ==============================  ==========================
+
+``raster_terrain`` is new: slope, aspect and hillshade from ONE pass over the
+DEM (the reference needs three calls and three passes).
+
+There is no CPU path.  ``use_gpu`` is accepted for signature compatibility;
+``use_gpu=False`` raises, and ``None`` always selects the GPU.
+"""
+
+from __future__ import annotations
+
+import math
+import time
+
+import numpy as np
+
+from vsr_gb300 import _lib
+from vsr_gb300.buffers import (
+    OwnedRasterArray,
+    RasterDiagnosticEvent,
+    RasterDiagnosticKind,
+    from_device,
+    torch_dtype,
+)
+from vsr_gb300.residency import Residency
+
+_GPU_ONLY = (
+    "vsr_gb300 runs focal operations on the GPU only; use the reference package "
+    "for its CPU path (use_gpu=False)"
+)
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def _should_use_gpu(raster: OwnedRasterArray, threshold: int = 10_000) -> bool:
+    """The reference's auto-dispatch test (algebra.py:3009-3019).
+
+    Kept for API parity; this package always runs on the GPU.
+    """
+    torch = _torch()
+    return bool(torch.cuda.is_available()) and raster.pixel_count >= threshold
+
+
+def _require_gpu(use_gpu) -> None:
+    if use_gpu is False:
+        raise NotImplementedError(_GPU_ONLY)
+    torch = _torch()
+    if not torch.cuda.is_available():
+        raise RuntimeError("vsr_gb300 needs a CUDA device (GB300, sm_103a)")
+    _lib.load()
+
+
+def _stream_handle():
+    return _torch().cuda.current_stream().cuda_stream
+
+
+def cellsize(affine) -> tuple[float, float]:
+    """|a|, |e| of the affine with 1.0 for zero (algebra.py:2307-2308)."""
+    a = float(affine[0])
+    e = float(affine[4])
+    return (abs(a) if a != 0 else 1.0, abs(e) if e != 0 else 1.0)
+
+
+def nodata_kind(raster: OwnedRasterArray) -> tuple[int, float]:
+    nd = raster.nodata
+    if nd is None:
+        return _lib.VSR_NODATA_NONE, 0.0
+    if isinstance(nd, float) and math.isnan(nd):
+        return _lib.VSR_NODATA_NAN, float("nan")
+    return _lib.VSR_NODATA_VALUE, float(nd)
+
+
+# Element types libvsr reads natively; others are widened exactly on the device.
+_WIDEN = {
+    np.dtype(np.int8): np.dtype(np.int16),
+    np.dtype(np.uint32): np.dtype(np.float64),
+    np.dtype(np.int64): np.dtype(np.float64),
+    np.dtype(np.uint64): np.dtype(np.float64),
+    np.dtype(np.float16): np.dtype(np.float32),
+    np.dtype(np.bool_): np.dtype(np.uint8),
+}
+
+
+def _device_bands(raster: OwnedRasterArray):
+    """(B, H, W) contiguous device tensor of a natively readable dtype."""
+    t = raster.device_data()
+    if t.ndim == 2:
+        t = t.unsqueeze(0)
+    dt = np.dtype(raster.dtype)
+    if dt in _WIDEN:
+        t = t.to(torch_dtype(_WIDEN[dt]))
+        dt = _WIDEN[dt]
+    if not t.is_contiguous():
+        t = t.contiguous()
+    return t, dt
+
+
+def _shape_like(raster: OwnedRasterArray, t):
+    """Return ``t`` (B, H, W) shaped like the input: 2-D when the input is 2-D."""
+    return t[0] if raster.data.ndim == 2 else t
+
+
+def _record(result: OwnedRasterArray, detail: str, elapsed: float = 0.0) -> OwnedRasterArray:
+    result.diagnostics.append(
+        RasterDiagnosticEvent(
+            kind=RasterDiagnosticKind.RUNTIME,
+            detail=detail,
+            residency=Residency.DEVICE,
+            visible_to_user=True,
+            elapsed_seconds=elapsed,
+        )
+    )
+    return result
+
+
+# ---------------------------------------------------------------------------
+# Horn 3x3 family
+# ---------------------------------------------------------------------------
+
+NODATA_WINDOW = "window"  # reference CPU rule (algebra.py:2218-2247); default
+NODATA_CENTER = "center"  # reference GPU kernel rule (kernels/focal.py:245-250)
+
+
+def _terrain_out_dtype(dt: np.dtype) -> np.dtype:
+    """float input keeps its dtype, anything else gives float64 (algebra.py:2419-2427)."""
+    dt = np.dtype(dt)
+    if np.issubdtype(dt, np.floating) and dt != np.float64:
+        return dt
+    return np.dtype(np.float64)
+
+
+def horn_fused(
+    dem: OwnedRasterArray,
+    *,
+    slope: bool = True,
+    aspect: bool = True,
+    hillshade: bool = True,
+    azimuth: float = 315.0,
+    altitude: float = 45.0,
+    z_factor: float = 1.0,
+    nodata_mode: str = NODATA_WINDOW,
+    out=None,
+):
+    """Launch vsr_horn_fused over every band; returns (slope, aspect, hs) tensors.
+
+    ``out`` may supply preallocated (B, H, W) device tensors for the three
+    outputs (None entries are allocated).
+    """
+    torch = _torch()
+    src, dt = _device_bands(dem)
+    B, H, W = src.shape
+    kind, ndv = nodata_kind(dem)
+    flags = 0
+    if nodata_mode == NODATA_CENTER:
+        flags |= _lib.VSR_HORN_CENTER_ONLY
+    elif nodata_mode != NODATA_WINDOW:
+        raise ValueError(f"nodata_mode must be 'window' or 'center', got {nodata_mode!r}")
+    else:
+        flags |= _lib.VSR_HORN_SA_NAN_UNMASKED
+    out_np = _terrain_out_dtype(dem.dtype)
+    compute_np = np.dtype(np.float64) if out_np == np.float64 else np.dtype(np.float32)
+    o_s, o_a, o_h = out if out is not None else (None, None, None)
+    dev = src.device
+    s_t = (o_s if o_s is not None else torch.empty((B, H, W), dtype=torch_dtype(compute_np), device=dev)) if slope else None
+    a_t = (o_a if o_a is not None else torch.empty((B, H, W), dtype=torch_dtype(compute_np), device=dev)) if aspect else None
+    h_t = (o_h if o_h is not None else torch.empty((B, H, W), dtype=torch.uint8, device=dev)) if hillshade else None
+    cx, cy = cellsize(dem.affine)
+    zen = math.radians(90.0 - float(altitude))
+    az = math.radians(float(azimuth))
+    lib = _lib.load()
+    code = _lib.dtype_code(dt)
+    ocode = _lib.VSR_F64 if compute_np == np.float64 else _lib.VSR_F32
+    stream = _stream_handle()
+    esz = src.element_size()
+    for b in range(B):
+        st = lib.vsr_horn_fused(
+            src.data_ptr() + b * H * W * esz, code, H, W, W, cx, cy, ndv, kind, flags,
+            s_t[b].data_ptr() if s_t is not None else None,
+            a_t[b].data_ptr() if a_t is not None else None,
+            ocode, W,
+            h_t[b].data_ptr() if h_t is not None else None, W,
+            float(z_factor), zen, az, stream,
+        )
+        _lib.check(st, "vsr_horn_fused")
+    if out_np not in (np.dtype(np.float32), np.dtype(np.float64)):
+        s_t = s_t.to(torch_dtype(out_np)) if s_t is not None else None
+        a_t = a_t.to(torch_dtype(out_np)) if a_t is not None else None
+    return s_t, a_t, h_t
+
+
+def raster_slope(dem: OwnedRasterArray, *, use_gpu: bool | None = None,
+                 nodata_mode: str = NODATA_WINDOW) -> OwnedRasterArray:
+    """Slope in degrees (Horn 3x3), reference algebra.py:2386-2459."""
+    _require_gpu(use_gpu)
+    t0 = time.perf_counter()
+    s, _, _ = horn_fused(dem, slope=True, aspect=False, hillshade=False, nodata_mode=nodata_mode)
+    res = from_device(_shape_like(dem, s), nodata=dem.nodata, affine=dem.affine, crs=dem.crs)
+    return _record(res, f"gpu_slope_fused {dem.width}x{dem.height}", time.perf_counter() - t0)
+
+
+def raster_aspect(dem: OwnedRasterArray, *, use_gpu: bool | None = None,
+                  nodata_mode: str = NODATA_WINDOW) -> OwnedRasterArray:
+    """Aspect in compass degrees (0 = north, clockwise), reference algebra.py:2462-2535."""
+    _require_gpu(use_gpu)
+    t0 = time.perf_counter()
+    _, a, _ = horn_fused(dem, slope=False, aspect=True, hillshade=False, nodata_mode=nodata_mode)
+    res = from_device(_shape_like(dem, a), nodata=dem.nodata, affine=dem.affine, crs=dem.crs)
+    return _record(res, f"gpu_aspect_fused {dem.width}x{dem.height}", time.perf_counter() - t0)
+
+
+def raster_hillshade(dem: OwnedRasterArray, *, azimuth: float = 315.0, altitude: float = 45.0,
+                     z_factor: float = 1.0, use_gpu: bool | None = None) -> OwnedRasterArray:
+    """uint8 hillshade, reference algebra.py:2778-2818 (nodata 0 if the input has nodata)."""
+    _require_gpu(use_gpu)
+    t0 = time.perf_counter()
+    _, _, h = horn_fused(dem, slope=False, aspect=False, hillshade=True, azimuth=azimuth,
+                         altitude=altitude, z_factor=z_factor)
+    res = from_device(_shape_like(dem, h), nodata=0 if dem.nodata is not None else None,
+                      affine=dem.affine, crs=dem.crs)
+    return _record(res, f"gpu_hillshade {dem.width}x{dem.height}", time.perf_counter() - t0)
+
+
+def raster_terrain(dem: OwnedRasterArray, *, slope: bool = True, aspect: bool = True, hillshade: bool = True,
+                   azimuth: float = 315.0, altitude: float = 45.0, z_factor: float = 1.0,
+                   nodata_mode: str = NODATA_WINDOW, use_gpu: bool | None = None) -> dict[str, OwnedRasterArray]:
+    """Slope, aspect and hillshade from one fused pass over the DEM.
+
+    Each result equals what raster_slope / raster_aspect / raster_hillshade
+    return for the same DEM; returns a dict with the requested keys.
+    """
+    _require_gpu(use_gpu)
+    t0 = time.perf_counter()
+    s, a, h = horn_fused(dem, slope=slope, aspect=aspect, hillshade=hillshade, azimuth=azimuth,
+                         altitude=altitude, z_factor=z_factor, nodata_mode=nodata_mode)
+    dt = time.perf_counter() - t0
+    out = {}
+    if s is not None:
+        out["slope"] = _record(from_device(_shape_like(dem, s), nodata=dem.nodata, affine=dem.affine, crs=dem.crs),
+                               f"gpu_slope_fused {dem.width}x{dem.height}", dt)
+    if a is not None:
+        out["aspect"] = _record(from_device(_shape_like(dem, a), nodata=dem.nodata, affine=dem.affine, crs=dem.crs),
+                                f"gpu_aspect_fused {dem.width}x{dem.height}", dt)
+    if h is not None:
+        out["hillshade"] = _record(
+            from_device(_shape_like(dem, h), nodata=0 if dem.nodata is not None else None, affine=dem.affine,
+                        crs=dem.crs),
+            f"gpu_hillshade {dem.width}x{dem.height}", dt)
+    return out
