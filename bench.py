@@ -189,7 +189,7 @@ def run_vsr(args, ws, rank, local):
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=dev)
-    dem = workloads.terrain_16k(device=dev)
+    dem = workloads.terrain_16k(device=dev, size=args.dem_size)
     H, W = dem.data.shape
     px = H * W
     r = vsr.from_device(dem.data, nodata=dem.nodata, affine=dem.affine)
@@ -282,7 +282,7 @@ def run_vsr(args, ws, rank, local):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "pixels": px, "bytes_per_pixel": BYTES_PER_PX,
+            "config": {"workload": WORKLOAD if H == 16384 else WORKLOAD.replace("16384x16384", f"{H}x{W}"), "pixels": px, "bytes_per_pixel": BYTES_PER_PX,
                        "l2": "inputs+outputs (3.5 GB/step) exceed L2; no flush",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
             "gpu_launches": args.steps,
@@ -307,6 +307,8 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["vsr", "reference"], default="vsr")
+    ap.add_argument("--dem-size", type=int, default=16384,
+                    help="DEM side (the benchmark workload is 16384; smaller sizes are for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

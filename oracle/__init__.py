@@ -21,6 +21,7 @@ from oracle.focal_oracle import (  # noqa: F401
     gaussian_weights,
     hillshade,
     nodata_mask,
+    nodata_ring,
     slope_aspect,
     slope_aspect_center_only,
     terrain_out_dtype,

@@ -124,6 +124,22 @@ def slope_aspect(data: np.ndarray, affine, nodata, *, compute_slope=True, comput
     return slope, aspect
 
 
+def nodata_ring(data: np.ndarray, nodata) -> np.ndarray:
+    """Pixels that the reference CPU slope/aspect set to nodata.
+
+    algebra.py:2186-2228: mask ``data == nodata`` (float64 compare; NaN never
+    matches), edge-padded, OR-ed over the 3x3 window.
+    """
+    z = np.asarray(data).astype(np.float64)
+    if nodata is None:
+        return np.zeros(z.shape, bool)
+    m = np.pad(z == float(nodata), 1, mode="edge")
+    ring = np.zeros(z.shape, bool)
+    for v in _shifted3x3(m):
+        ring |= v
+    return ring
+
+
 def slope_aspect_center_only(data: np.ndarray, affine, nodata):
     """Reference GPU slope/aspect semantics, kernels/focal.py:173-283.
 
