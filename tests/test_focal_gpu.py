@@ -1,0 +1,145 @@
+"""GPU parity of normalised convolution, Gaussian and focal mean vs the oracle.
+
+Tolerances: convolution and Gaussian within 1e-5 relative of the float64
+oracle (the path's stated bound) -- measured as |out - ref| <= 1e-5 * max(|ref|,
+scale) with ``scale`` the mean |value| of the input, so that outputs that
+cancel to ~0 are judged against the data's magnitude; nodata / NaN placement
+exact.  Focal mean: integer rasters exactly rounded (sums are exact), float
+rasters within 1e-12 relative (compensated float32 sums).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-5
+
+
+def _assert_close(out, ref, data, nodata, rel=REL):
+    out = np.asarray(out, np.float64)
+    ref = np.asarray(ref, np.float64)
+    np.testing.assert_array_equal(np.isnan(out), np.isnan(ref))
+    m = ~np.isnan(ref)
+    if nodata is not None and not np.isnan(nodata):
+        np.testing.assert_array_equal(out[m] == nodata, ref[m] == nodata)
+    scale = float(np.nanmean(np.abs(np.asarray(data, np.float64)))) or 1.0
+    err = np.abs(out[m] - ref[m])
+    bound = rel * np.maximum(np.abs(ref[m]), scale)
+    assert (err <= bound).all(), f"max rel err {np.max(err / np.maximum(np.abs(ref[m]), scale)):.3e}"
+
+
+@pytest.mark.parametrize("shape,k,nodata", [
+    ((37, 53), (3, 3), None), ((64, 128), (5, 5), -9999.0), ((129, 257), (15, 15), None),
+    ((100, 300), (31, 31), -9999.0), ((70, 90), (7, 3), float("nan")), ((33, 40), (2, 4), None),
+    ((1, 50), (3, 3), None), ((50, 1), (5, 5), -1.0), ((200, 150), (41, 41), None), ((65, 70), (65, 65), 0.0),
+])
+def test_convolve_vs_oracle(vsr, shape, k, nodata):
+    rng = np.random.default_rng(sum(shape) + k[0])
+    d = (rng.random(shape) + np.linspace(0, 100, shape[0] * shape[1]).reshape(shape)).astype(np.float32)
+    if nodata is not None:
+        d[rng.random(shape) < 0.03] = nodata
+    w = rng.random(k)
+    w /= w.sum()
+    r = vsr.from_numpy(d, nodata=nodata)
+    out = vsr.raster_convolve(r, w, precision="fp32")
+    assert out.dtype == np.float64 and out.nodata == nodata
+    _assert_close(out.to_numpy(), oracle.convolve_normalized(d, w, nodata), d, nodata)
+
+
+def test_convolve_signed_and_zero_sum_kernels(vsr):
+    rng = np.random.default_rng(4)
+    d = rng.uniform(-10, 10, (40, 60)).astype(np.float32)
+    for w in (np.array([[1.0, 0.0, -1.0]]), rng.uniform(-1, 1, (5, 5)), np.ones((1, 1))):
+        out = vsr.raster_convolve(vsr.from_numpy(d), w, precision="fp32").to_numpy()
+        ref = oracle.convolve_normalized(d, w, None)
+        # signed kernels cancel; judge against the data's magnitude
+        np.testing.assert_allclose(out, ref, rtol=1e-4, atol=1e-4 * np.abs(d).mean())
+
+
+def test_convolve_known_answers(vsr):
+    """Reference tests/test_raster_algebra.py:372-418, through the GPU path."""
+    d = np.arange(30, dtype=np.float32).reshape(5, 6)
+    np.testing.assert_array_equal(vsr.raster_convolve(vsr.from_numpy(d), np.ones((1, 1))).to_numpy(), d)
+    ones = vsr.from_numpy(np.ones((8, 8), np.float32))
+    np.testing.assert_allclose(vsr.raster_convolve(ones, np.ones((3, 3)) / 9.0).to_numpy(), 1.0, rtol=1e-6)
+    with pytest.raises(ValueError, match="kernel must be 2D"):
+        vsr.raster_convolve(ones, np.ones(3))
+    imp = np.zeros((11, 11), np.float32)
+    imp[5, 5] = 100.0
+    g = vsr.raster_gaussian_filter(vsr.from_numpy(imp), 1.0).to_numpy()
+    assert g[5, 5] < 100.0 and g[5, 6] > 0.0 and g[4, 5] > 0.0
+    with pytest.raises(ValueError, match="sigma must be positive"):
+        vsr.raster_gaussian_filter(ones, 0.0)
+    assert any(e.detail.startswith("gpu_convolve") for e in vsr.raster_convolve(ones, np.ones((3, 3))).diagnostics)
+
+
+@pytest.mark.parametrize("sigma,ks,nodata", [(1.0, 5, None), (1.0, 5, float("nan")), (1.0, None, -9999.0),
+                                             (2.5, 8, None), (5.0, 41, -9999.0), (3.0, None, 0.0),
+                                             (8.0, 65, -9999.0)])
+def test_gaussian_vs_oracle(vsr, golden, sigma, ks, nodata):
+    arrays, manifest = golden
+    rng = np.random.default_rng(int(sigma * 10))
+    shape = (150, 210)
+    d = (rng.random(shape) * 5 + np.linspace(0, 100, shape[0] * shape[1]).reshape(shape)).astype(np.float32)
+    if nodata is not None:
+        d[rng.random(shape) < 0.02] = nodata
+    # the reference's own weights for this (sigma, kernel_size)
+    key = f"gaussian/s{sigma}_k{ks}"
+    w = arrays[key] if key in arrays.files else oracle.gaussian_weights(sigma, ks)
+    ref = oracle.convolve_normalized(d, w, nodata)
+    out = vsr.raster_gaussian_filter(vsr.from_numpy(d, nodata=nodata), sigma, kernel_size=ks, precision="fp32")
+    _assert_close(out.to_numpy(), ref, d, nodata)
+
+
+def test_gaussian_multiband_equals_per_band(vsr):
+    rng = np.random.default_rng(1)
+    stack = rng.random((3, 40, 70)).astype(np.float32)
+    out = vsr.raster_gaussian_filter(vsr.from_numpy(stack), 1.0, kernel_size=5).to_numpy()
+    for b in range(3):
+        ob = vsr.raster_gaussian_filter(vsr.from_numpy(stack[b]), 1.0, kernel_size=5).to_numpy()
+        np.testing.assert_array_equal(out[b], ob)
+
+
+def test_focal_mean_golden(vsr, golden):
+    arrays, manifest = golden
+    for case in manifest["focal_mean"]:
+        name = case["name"]
+        data = arrays[f"focal_mean/{name}/input"]
+        ref = arrays[f"focal_mean/{name}/output"]
+        out = vsr.raster_focal_mean(vsr.from_numpy(data, nodata=case["nodata"]), tuple(case["radius"])).to_numpy()
+        assert out.dtype == np.float64
+        np.testing.assert_allclose(out, ref, rtol=1e-12, atol=1e-12, err_msg=name)
+
+
+@pytest.mark.parametrize("dtype,nodata,radius", [(np.uint16, 0, 3), (np.float32, -9999.0, (1, 2)),
+                                                 (np.float32, float("nan"), 2), (np.int16, -32768, 1),
+                                                 (np.float64, None, 3), (np.uint8, 255, (2, 0))])
+def test_focal_mean_vs_oracle(vsr, dtype, nodata, radius):
+    rng = np.random.default_rng(5)
+    shape = (97, 301)
+    if np.issubdtype(dtype, np.integer):
+        d = rng.integers(0, 250 if dtype == np.uint8 else 10000, shape).astype(dtype)
+    else:
+        d = rng.uniform(-100, 4000, shape).astype(dtype)
+    if nodata is not None:
+        d[rng.random(shape) < 0.05] = nodata
+    ry, rx = (radius, radius) if isinstance(radius, int) else radius
+    out = vsr.raster_focal_mean(vsr.from_numpy(d, nodata=nodata), radius).to_numpy()
+    ref = oracle.focal_mean(d, ry, rx, nodata)
+    if np.issubdtype(dtype, np.integer):
+        np.testing.assert_array_equal(out, ref)  # exact sums, one float64 division
+    else:
+        np.testing.assert_allclose(out, ref, rtol=1e-12, atol=1e-9)
+
+
+def test_focal_mean_known_answer(vsr):
+    """Reference tests/test_focal_stats.py:113-127: 1..25 5x5, centre mean 13."""
+    d = np.arange(1, 26, dtype=np.float64).reshape(5, 5)
+    out = vsr.raster_focal_mean(vsr.from_numpy(d), 1).to_numpy()
+    assert out[2, 2] == 13.0
+    assert any(e.detail.startswith("gpu_focal_mean") for e in vsr.raster_focal_mean(vsr.from_numpy(d), 1).diagnostics)

@@ -142,11 +142,17 @@ def test_center_only_mode_matches_reference_gpu_rule(vsr):
     a = vsr.raster_aspect(r, nodata_mode="center").to_numpy()
     rs, ra = oracle.slope_aspect_center_only(d, aff, -9999.0)
     np.testing.assert_array_equal(s == -9999.0, rs == -9999.0)
-    m = rs != -9999.0
-    # neighbours' raw -9999 enter the gradient here, so compare relative to the
-    # gradient scale (slope is near 90 degrees around holes)
-    assert np.abs(s[m] - rs[m]).max() <= TOL_DEG
-    assert _circ(a[m], ra[m]).max() <= 1e-3
+    ring = oracle.nodata_ring(d, -9999.0)
+    clean = ~ring
+    # windows without nodata: the path's 1e-4 degree bound
+    assert np.abs(s[clean] - rs[clean]).max() <= TOL_DEG
+    assert _circ(a[clean], ra[clean]).max() <= TOL_DEG
+    # windows where the raw -9999 enters the gradient (this mode's defining
+    # quirk): differences of ~1e4 m cancel, so float32 keeps ~1e-3 m of each
+    # term; the bound is correspondingly looser
+    m = ring & (rs != -9999.0)
+    assert np.abs(s[m] - rs[m]).max() <= 1e-2
+    assert _circ(a[m], ra[m]).max() <= 1e-2
 
 
 def test_multiband_equals_per_band(vsr):

@@ -1,28 +1,700 @@
-// Focal convolution, Gaussian and focal mean entry points.
+// Focal convolution (plain FP32), Gaussian filter and focal mean.
+//
+// * conv_direct  -- nodata-aware normalised correlation (kernels/focal.py:
+//   36-146 of the reference).  A CTA stages a (32 + kh - 1) x (128 + kw - 1)
+//   tile of v*valid and valid into shared memory (v*valid keeps the
+//   reference's NaN * 0 = NaN poisoning), then each thread accumulates a
+//   4 x 4 register block of outputs with a register window sliding along the
+//   row (kernel width bucketed at compile time, the loop guarded by the
+//   runtime width), one row partial sum per kernel row (for accuracy) and
+//   16-byte broadcast weight loads.  The weight-sum pass runs only on tiles
+//   that touch the border or hold nodata; other tiles use the full sum.
+// * sep_tile     -- the Gaussian as two 1-D passes inside one CTA: the row
+//   pass over the staged tile is held in shared memory and the column pass
+//   reads it.  Numerator and weight sum are both separable, so this equals
+//   the reference's dense k x k normalised correlation with weights
+//   outer(g, g)/sum in real arithmetic, border and nodata handling included.
+// * box_mean     -- focal mean as exact separable sums: int32 for <= 16-bit
+//   integer rasters, float TwoSum pairs for float32, float64 otherwise;
+//   mean = sum / count formed in float64 (reference: Welford in float64,
+//   kernels/focal.py:672-769 / scipy generic_filter, algebra.py:3083-3101).
+#include <algorithm>
+
 #include "vsr_internal.cuh"
+
+namespace vsr {
+namespace {
+
+// ------------------------------------------------------------ element IO --
+struct NodataSpec {
+  int kind;     // resolved VSR_NODATA_*
+  float fv;     // value as float (float32 rasters)
+  double dv;    // value as double (float64 rasters)
+  int64_t iv;   // value as integer (integer rasters)
+};
+
+// Load element ``idx`` of a raster of ``dtype``; returns the value as float
+// and sets ``valid`` (not nodata).
+__device__ __forceinline__ float load_elem(const void* base, int dtype, int64_t idx,
+                                           const NodataSpec& nd, bool& valid) {
+  switch (dtype) {
+    case VSR_F32: {
+      const float v = __ldg(static_cast<const float*>(base) + idx);
+      valid = !(nd.kind == VSR_NODATA_VALUE ? v == nd.fv : (nd.kind == VSR_NODATA_NAN ? v != v : false));
+      return v;
+    }
+    case VSR_F64: {
+      const double v = __ldg(static_cast<const double*>(base) + idx);
+      valid = !(nd.kind == VSR_NODATA_VALUE ? v == nd.dv : (nd.kind == VSR_NODATA_NAN ? v != v : false));
+      return static_cast<float>(v);
+    }
+    case VSR_U8: {
+      const int v = __ldg(static_cast<const uint8_t*>(base) + idx);
+      valid = !(nd.kind == VSR_NODATA_VALUE && v == nd.iv);
+      return static_cast<float>(v);
+    }
+    case VSR_I16: {
+      const int v = __ldg(static_cast<const int16_t*>(base) + idx);
+      valid = !(nd.kind == VSR_NODATA_VALUE && v == nd.iv);
+      return static_cast<float>(v);
+    }
+    case VSR_U16: {
+      const int v = __ldg(static_cast<const uint16_t*>(base) + idx);
+      valid = !(nd.kind == VSR_NODATA_VALUE && v == nd.iv);
+      return static_cast<float>(v);
+    }
+    default: {
+      const int v = __ldg(static_cast<const int32_t*>(base) + idx);
+      valid = !(nd.kind == VSR_NODATA_VALUE && v == nd.iv);
+      return static_cast<float>(v);
+    }
+  }
+}
+
+__device__ __forceinline__ void store_out(void* dst, int out_dtype, int64_t idx, double v) {
+  if (out_dtype == VSR_F64) static_cast<double*>(dst)[idx] = v;
+  else static_cast<float*>(dst)[idx] = static_cast<float>(v);
+}
+
+NodataSpec make_nodata(int dtype, double nodata, int kind) {
+  NodataSpec s{};
+  double ev = 0.0;
+  s.kind = resolve_nodata(dtype, nodata, kind, &ev);
+  s.dv = ev;
+  s.fv = static_cast<float>(ev);
+  s.iv = static_cast<int64_t>(ev);
+  return s;
+}
+
+// Bank-spreading position inside a staged row: one pad word per 32 floats,
+// so lanes reading 4 columns apart hit distinct banks.
+__device__ __forceinline__ int pos(int c) { return c + (c >> 5); }
+__host__ __device__ inline int padded_width(int w) { return w + (w >> 5) + 1; }
+
+// ---------------------------------------------------------- weight prep --
+// float64 weights -> float32 rows padded to a multiple of 4 (zero fill) and
+// the float64 total.  One CTA.
+__global__ void prep_weights(const double* __restrict__ w64, int kh, int kw, int kw4,
+                             float* __restrict__ w32, float* __restrict__ wsum) {
+  __shared__ double part[256];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < kh * kw4; i += blockDim.x) {
+    const int r = i / kw4, c = i % kw4;
+    const double v = c < kw ? w64[r * kw + c] : 0.0;
+    w32[i] = static_cast<float>(v);
+    acc += v;
+  }
+  part[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) part[threadIdx.x] += part[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) wsum[0] = static_cast<float>(part[0]);
+}
+
+// Gaussian weights in float64 on the device: g_i = exp(-0.5 ((i - k/2)/sigma)^2),
+// as float32 g (1-D, padded to a multiple of 4) and, when ``w2`` is given,
+// the dense outer(g, g) / sum as float32 rows padded to k4 (the reference's
+// weights, algebra.py:2149-2152) plus its float64 total.
+__global__ void prep_gaussian(int k, int k4, double sigma, float* __restrict__ g32,
+                              float* __restrict__ w2, float* __restrict__ wsum) {
+  extern __shared__ double g64[];
+  for (int i = threadIdx.x; i < k; i += blockDim.x) {
+    const double a = (i - k / 2) / sigma;
+    g64[i] = exp(-0.5 * a * a);
+  }
+  __syncthreads();
+  __shared__ double total;
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < k; ++i) s += g64[i];
+    total = s * s;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < k4; i += blockDim.x) g32[i] = i < k ? static_cast<float>(g64[i]) : 0.0f;
+  if (w2) {
+    for (int i = threadIdx.x; i < k * k4; i += blockDim.x) {
+      const int r = i / k4, c = i % k4;
+      w2[i] = c < k ? static_cast<float>(g64[r] * g64[c] / total) : 0.0f;
+    }
+    if (threadIdx.x == 0) wsum[0] = 1.0f;
+  }
+}
+
+// ---------------------------------------------------------- conv_direct --
+constexpr int kCRX = 4, kCRY = 4;            // outputs per thread (x, y)
+constexpr int kCTW = 32 * kCRX, kCTH = 8 * kCRY;  // 128 x 32 tile, 256 threads
+
+struct ConvArgs {
+  const void* src;
+  int dtype;
+  int64_t H, W, pitch;
+  NodataSpec nd;
+  const float* w32;   // kh x kw4
+  const float* wsum;  // total weight (float)
+  int kh, kw, kw4;
+  double nd_out;
+  void* dst;
+  int out_dtype;
+  int64_t out_pitch;
+};
+
+inline size_t conv_smem_bytes(int kh, int kw) {
+  const int SH = kCTH + kh - 1, SW = kCTW + kw - 1;
+  const int kw4 = (kw + 3) & ~3;
+  return static_cast<size_t>(2 * SH * padded_width(SW) + kh * kw4) * 4 + 16;
+}
+
+// One pass of register-blocked correlation over plane ``P`` (v*valid or valid).
+template <int MAXW>
+__device__ __forceinline__ void conv_accumulate(const float* __restrict__ P, int PW,
+                                                const float* __restrict__ wt, int kh, int kw, int kw4,
+                                                int r0, int c0, float acc[kCRY][kCRX]) {
+  for (int iy = 0; iy < kCRY + kh - 1; ++iy) {
+    float V[kCRX + MAXW - 1];
+    const float* row = P + (r0 + iy) * PW;
+#pragma unroll
+    for (int j = 0; j < kCRX + MAXW - 1; ++j)
+      V[j] = (j < kCRX + kw - 1) ? row[pos(c0 + j)] : 0.0f;
+#pragma unroll
+    for (int ry = 0; ry < kCRY; ++ry) {
+      const int ky = iy - ry;
+      if (ky < 0 || ky >= kh) continue;
+      const float* wr = wt + ky * kw4;
+      float part[kCRX] = {};
+#pragma unroll
+      for (int kx = 0; kx < MAXW; kx += 4) {
+        if (kx >= kw) break;
+        const float4 w4 = *reinterpret_cast<const float4*>(wr + kx);
+        const float wv[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          // never multiply a zero pad weight: a NaN outside this output's
+          // window must not leak in through 0 * NaN
+          if (kx + u < kw) {
+#pragma unroll
+            for (int rx = 0; rx < kCRX; ++rx) part[rx] = fmaf(wv[u], V[rx + kx + u], part[rx]);
+          }
+        }
+      }
+#pragma unroll
+      for (int rx = 0; rx < kCRX; ++rx) acc[ry][rx] += part[rx];
+    }
+  }
+}
+
+template <int MAXW>
+__global__ void __launch_bounds__(256) conv_direct(const ConvArgs a) {
+  extern __shared__ __align__(16) float smem[];
+  const int SH = kCTH + a.kh - 1, SW = kCTW + a.kw - 1, PW = padded_width(SW);
+  float* vz = smem;
+  float* vd = vz + SH * PW;
+  float* wt = vd + SH * PW;  // 16-byte aligned: SH*PW*2 floats precede it
+  // keep wt 16-byte aligned
+  wt = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(wt) + 15) & ~uintptr_t(15));
+  const int tid = threadIdx.y * 32 + threadIdx.x;
+  const int64_t x0 = static_cast<int64_t>(blockIdx.x) * kCTW;
+  const int64_t y0 = static_cast<int64_t>(blockIdx.y) * kCTH;
+  const int px = a.kw / 2, py = a.kh / 2;
+
+  for (int i = tid; i < a.kh * a.kw4; i += 256) wt[i] = a.w32[i];
+  bool any_gap = false;
+  for (int i = tid; i < SH * SW; i += 256) {
+    const int r = i / SW, c = i - r * SW;
+    const int64_t gy = y0 + r - py, gx = x0 + c - px;
+    float v = 0.0f, d = 0.0f;
+    if (gy >= 0 && gy < a.H && gx >= 0 && gx < a.W) {
+      bool ok;
+      const float x = load_elem(a.src, a.dtype, gy * a.pitch + gx, a.nd, ok);
+      v = x * (ok ? 1.0f : 0.0f);  // NaN * 0 stays NaN, as in the reference
+      d = ok ? 1.0f : 0.0f;
+      any_gap |= !ok;
+    } else {
+      any_gap = true;
+    }
+    vz[r * PW + pos(c)] = v;
+    vd[r * PW + pos(c)] = d;
+  }
+  const bool need_den = __syncthreads_or(any_gap);
+
+  const int r0 = threadIdx.y * kCRY, c0 = threadIdx.x * kCRX;
+  float num[kCRY][kCRX] = {};
+  conv_accumulate<MAXW>(vz, PW, wt, a.kh, a.kw, a.kw4, r0, c0, num);
+  float den[kCRY][kCRX];
+  if (need_den) {
+#pragma unroll
+    for (int ry = 0; ry < kCRY; ++ry)
+#pragma unroll
+      for (int rx = 0; rx < kCRX; ++rx) den[ry][rx] = 0.0f;
+    conv_accumulate<MAXW>(vd, PW, wt, a.kh, a.kw, a.kw4, r0, c0, den);
+  } else {
+    const float ws = *a.wsum;
+#pragma unroll
+    for (int ry = 0; ry < kCRY; ++ry)
+#pragma unroll
+      for (int rx = 0; rx < kCRX; ++rx) den[ry][rx] = ws;
+  }
+#pragma unroll
+  for (int ry = 0; ry < kCRY; ++ry) {
+    const int64_t y = y0 + r0 + ry;
+    if (y >= a.H) break;
+#pragma unroll
+    for (int rx = 0; rx < kCRX; ++rx) {
+      const int64_t x = x0 + c0 + rx;
+      if (x >= a.W) break;
+      const bool centre_ok = vd[(r0 + ry + py) * PW + pos(c0 + rx + px)] != 0.0f;
+      const float dn = den[ry][rx];
+      const double out = (centre_ok && dn > 0.0f) ? static_cast<double>(num[ry][rx] / dn) : a.nd_out;
+      store_out(a.dst, a.out_dtype, y * a.out_pitch + x, out);
+    }
+  }
+}
+
+template <int MAXW>
+int launch_conv_direct(const ConvArgs& a, cudaStream_t st) {
+  const size_t smem = conv_smem_bytes(a.kh, a.kw);
+  auto kern = conv_direct<MAXW>;
+  VSR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  dim3 grid(static_cast<unsigned>((a.W + kCTW - 1) / kCTW), static_cast<unsigned>((a.H + kCTH - 1) / kCTH));
+  if (grid.y > 65535u) return fail(VSR_ERR_UNSUPPORTED, "raster too tall for the direct convolution grid");
+  kern<<<grid, dim3(32, 8), smem, st>>>(a);
+  VSR_CUDA_TRY(cudaGetLastError());
+  return VSR_OK;
+}
+
+int run_conv_direct(const ConvArgs& a, cudaStream_t st) {
+  if (a.kw <= 4) return launch_conv_direct<4>(a, st);
+  if (a.kw <= 8) return launch_conv_direct<8>(a, st);
+  if (a.kw <= 16) return launch_conv_direct<16>(a, st);
+  if (a.kw <= 32) return launch_conv_direct<32>(a, st);
+  if (a.kw <= 48) return launch_conv_direct<48>(a, st);
+  if (a.kw <= 64) return launch_conv_direct<64>(a, st);
+  return launch_conv_direct<80>(a, st);
+}
+
+constexpr int kMaxDirectK = 80;
+
+// ------------------------------------------------------------- sep_tile --
+// Separable Gaussian for k <= 33 within a 128 x 32 output tile.
+constexpr int kSTW = 128, kSTH = 32;
+
+struct SepArgs {
+  const void* src;
+  int dtype;
+  int64_t H, W, pitch;
+  NodataSpec nd;
+  const float* g32;  // k4 floats
+  int k;
+  double nd_out;
+  void* dst;
+  int out_dtype;
+  int64_t out_pitch;
+};
+
+inline size_t sep_smem_bytes(int k) {
+  const int SH = kSTH + k - 1, SW = kSTW + k - 1;
+  // staged v*valid and valid, row-pass numerator and denominator, weights
+  return static_cast<size_t>(((2 * SH * padded_width(SW) + 3) & ~3) + 2 * SH * kSTW + ((k + 3) & ~3)) * 4 + 16;
+}
+
+template <int MAXK>
+__global__ void __launch_bounds__(256) sep_tile(const SepArgs a) {
+  extern __shared__ __align__(16) float smem[];
+  const int k = a.k, r = k / 2;
+  const int SH = kSTH + k - 1, SW = kSTW + k - 1, PW = padded_width(SW);
+  float* vz = smem;
+  float* vd = vz + SH * PW;
+  float* rn = vz + ((2 * SH * PW + 3) & ~3);  // SH x kSTW row-pass numerator (16-byte aligned)
+  float* rd = rn + SH * kSTW;
+  float* g = rd + SH * kSTW;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t x0 = static_cast<int64_t>(blockIdx.x) * kSTW;
+  const int64_t y0 = static_cast<int64_t>(blockIdx.y) * kSTH;
+
+  for (int i = tid; i < k; i += 256) g[i] = a.g32[i];
+  for (int i = tid; i < SH * SW; i += 256) {
+    const int rr = i / SW, c = i - rr * SW;
+    const int64_t gy = y0 + rr - r, gx = x0 + c - r;
+    float v = 0.0f, d = 0.0f;
+    if (gy >= 0 && gy < a.H && gx >= 0 && gx < a.W) {
+      bool ok;
+      const float x = load_elem(a.src, a.dtype, gy * a.pitch + gx, a.nd, ok);
+      v = x * (ok ? 1.0f : 0.0f);
+      d = ok ? 1.0f : 0.0f;
+    }
+    vz[rr * PW + pos(c)] = v;
+    vd[rr * PW + pos(c)] = d;
+  }
+  __syncthreads();
+
+  // Row pass: each lane 4 adjacent columns of one staged row.
+  for (int rr = warp; rr < SH; rr += 8) {
+    const int c0 = 4 * lane;
+#pragma unroll
+    for (int plane = 0; plane < 2; ++plane) {
+      const float* row = (plane == 0 ? vz : vd) + rr * PW;
+      float V[4 + MAXK - 1];
+#pragma unroll
+      for (int j = 0; j < 4 + MAXK - 1; ++j) V[j] = (j < 4 + k - 1) ? row[pos(c0 + j)] : 0.0f;
+      float acc[4] = {};
+#pragma unroll
+      for (int t = 0; t < MAXK; ++t) {
+        if (t >= k) break;
+        const float w = g[t];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) acc[u] = fmaf(w, V[u + t], acc[u]);
+      }
+      float* o = (plane == 0 ? rn : rd) + rr * kSTW + c0;
+      *reinterpret_cast<float4*>(o) = make_float4(acc[0], acc[1], acc[2], acc[3]);
+    }
+  }
+  __syncthreads();
+
+  // Column pass: each thread one column, 16 consecutive output rows.
+  constexpr int RY = kSTH / 2;
+  const int c = tid & (kSTW - 1);
+  const int q0 = (tid >> 7) * RY;
+  float num[RY] = {}, den[RY] = {};
+#pragma unroll
+  for (int plane = 0; plane < 2; ++plane) {
+    const float* P = plane == 0 ? rn : rd;
+    float* acc = plane == 0 ? num : den;
+    for (int i = 0; i < RY + k - 1; ++i) {
+      const float v = P[(q0 + i) * kSTW + c];
+#pragma unroll
+      for (int ry = 0; ry < RY; ++ry) {
+        const int t = i - ry;
+        if (t >= 0 && t < k) acc[ry] = fmaf(g[t], v, acc[ry]);
+      }
+    }
+  }
+  const int64_t x = x0 + c;
+  if (x < a.W) {
+#pragma unroll
+    for (int ry = 0; ry < RY; ++ry) {
+      const int64_t y = y0 + q0 + ry;
+      if (y >= a.H) break;
+      const bool centre_ok = vd[(q0 + ry + r) * PW + pos(c + r)] != 0.0f;
+      const double out = (centre_ok && den[ry] > 0.0f) ? static_cast<double>(num[ry] / den[ry]) : a.nd_out;
+      store_out(a.dst, a.out_dtype, y * a.out_pitch + x, out);
+    }
+  }
+}
+
+template <int MAXK>
+int launch_sep(const SepArgs& a, cudaStream_t st) {
+  const size_t smem = sep_smem_bytes(a.k);
+  auto kern = sep_tile<MAXK>;
+  VSR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  dim3 grid(static_cast<unsigned>((a.W + kSTW - 1) / kSTW), static_cast<unsigned>((a.H + kSTH - 1) / kSTH));
+  if (grid.y > 65535u) return fail(VSR_ERR_UNSUPPORTED, "raster too tall for the separable Gaussian grid");
+  kern<<<grid, 256, smem, st>>>(a);
+  VSR_CUDA_TRY(cudaGetLastError());
+  return VSR_OK;
+}
+
+constexpr int kMaxSepK = 33;
+
+// ------------------------------------------------------------- box_mean --
+// Accumulators: exact int32 sums (<= 16-bit integer rasters), float TwoSum
+// pairs (float32), float64 (float64 / int32 rasters).
+struct AccI {
+  int32_t s;
+  __device__ void zero() { s = 0; }
+  __device__ void add(int32_t v) { s += v; }
+  __device__ void add(const AccI& o) { s += o.s; }
+  __device__ double value() const { return static_cast<double>(s); }
+};
+struct AccF2 {
+  float s, c;
+  __device__ void zero() { s = 0.0f; c = 0.0f; }
+  __device__ void add_term(float v) {
+    // TwoSum (Knuth): s + v = t + e exactly
+    const float t = s + v;
+    const float bp = t - s;
+    const float e = (s - (t - bp)) + (v - bp);
+    s = t;
+    c += e;
+  }
+  __device__ void add(float v) { add_term(v); }
+  __device__ void add(const AccF2& o) { add_term(o.s); c += o.c; }
+  __device__ double value() const { return static_cast<double>(s) + static_cast<double>(c); }
+};
+struct AccD {
+  double s;
+  __device__ void zero() { s = 0.0; }
+  __device__ void add(double v) { s += v; }
+  __device__ void add(const AccD& o) { s += o.s; }
+  __device__ double value() const { return s; }
+};
+
+constexpr int kBTW = 128, kBTH = 32;
+
+struct BoxArgs {
+  const void* src;
+  int dtype;
+  int64_t H, W, pitch;
+  NodataSpec nd;
+  int ry, rx;
+  double nd_out;
+  void* dst;
+  int out_dtype;
+  int64_t out_pitch;
+};
+
+template <class Acc>
+inline size_t box_smem_bytes(int ry, int rx) {
+  const int SH = kBTH + 2 * ry, SW = kBTW + 2 * rx;
+  // staged value (as Acc input) + valid byte; row sums (Acc) + row counts (int)
+  return static_cast<size_t>(SH) * SW * (sizeof(double) + 1) + static_cast<size_t>(SH) * kBTW * (sizeof(Acc) + 4) + 64;
+}
+
+// Element value for the accumulator: exact for every supported dtype.
+template <class Acc>
+__device__ __forceinline__ double box_load(const void* base, int dtype, int64_t idx, const NodataSpec& nd,
+                                           bool& valid) {
+  if (dtype == VSR_F64) {
+    const double v = __ldg(static_cast<const double*>(base) + idx);
+    valid = !(nd.kind == VSR_NODATA_VALUE ? v == nd.dv : false) && v == v;
+    return v;
+  }
+  if (dtype == VSR_I32) {
+    const int32_t v = __ldg(static_cast<const int32_t*>(base) + idx);
+    valid = !(nd.kind == VSR_NODATA_VALUE && v == nd.iv);
+    return static_cast<double>(v);
+  }
+  const float v = load_elem(base, dtype, idx, nd, valid);
+  valid = valid && (v == v);  // NaN never counts (reference CPU mean excludes it)
+  return static_cast<double>(v);
+}
+
+template <class Acc>
+__global__ void __launch_bounds__(256) box_mean(const BoxArgs a) {
+  extern __shared__ __align__(16) unsigned char braw[];
+  const int SH = kBTH + 2 * a.ry, SW = kBTW + 2 * a.rx;
+  double* sv = reinterpret_cast<double*>(braw);                 // SH x SW values
+  Acc* rs = reinterpret_cast<Acc*>(sv + SH * SW);               // SH x kBTW row sums
+  int32_t* rc = reinterpret_cast<int32_t*>(rs + SH * kBTW);     // SH x kBTW row counts
+  uint8_t* sd = reinterpret_cast<uint8_t*>(rc + SH * kBTW);     // SH x SW valid
+  const int tid = threadIdx.x;
+  const int64_t x0 = static_cast<int64_t>(blockIdx.x) * kBTW;
+  const int64_t y0 = static_cast<int64_t>(blockIdx.y) * kBTH;
+
+  for (int i = tid; i < SH * SW; i += 256) {
+    const int rr = i / SW, c = i - rr * SW;
+    const int64_t gy = y0 + rr - a.ry, gx = x0 + c - a.rx;
+    double v = 0.0;
+    bool ok = false;
+    if (gy >= 0 && gy < a.H && gx >= 0 && gx < a.W) v = box_load<Acc>(a.src, a.dtype, gy * a.pitch + gx, a.nd, ok);
+    sv[i] = ok ? v : 0.0;
+    sd[i] = ok ? 1 : 0;
+  }
+  __syncthreads();
+  const int wx = 2 * a.rx + 1, wy = 2 * a.ry + 1;
+  for (int i = tid; i < SH * kBTW; i += 256) {
+    const int rr = i / kBTW, c = i - rr * kBTW;
+    Acc s;
+    s.zero();
+    int n = 0;
+    const double* row = sv + rr * SW + c;
+    const uint8_t* drow = sd + rr * SW + c;
+    for (int t = 0; t < wx; ++t) {
+      s.add(static_cast<decltype(Acc::s)>(row[t]));
+      n += drow[t];
+    }
+    rs[i] = s;
+    rc[i] = n;
+  }
+  __syncthreads();
+  for (int i = tid; i < kBTH * kBTW; i += 256) {
+    const int q = i / kBTW, c = i - q * kBTW;
+    const int64_t y = y0 + q, x = x0 + c;
+    if (y >= a.H || x >= a.W) continue;
+    Acc s;
+    s.zero();
+    int n = 0;
+    for (int t = 0; t < wy; ++t) {
+      s.add(rs[(q + t) * kBTW + c]);
+      n += rc[(q + t) * kBTW + c];
+    }
+    // The reference masks only nodata centres (algebra.py:3099-3100); a NaN
+    // centre that is not the nodata value still gets its window mean.
+    bool centre_ok = true;
+    if (a.nd.kind != VSR_NODATA_NONE) (void)load_elem(a.src, a.dtype, y * a.pitch + x, a.nd, centre_ok);
+    const bool centre_nodata = !centre_ok;
+    const double out = (centre_nodata || n == 0) ? a.nd_out : s.value() / static_cast<double>(n);
+    store_out(a.dst, a.out_dtype, y * a.out_pitch + x, out);
+  }
+}
+
+template <class Acc>
+int launch_box(const BoxArgs& a, cudaStream_t st) {
+  const size_t smem = box_smem_bytes<Acc>(a.ry, a.rx);
+  if (smem > 227 * 1024) return fail(VSR_ERR_UNSUPPORTED, "focal mean radius (%d, %d) too large", a.ry, a.rx);
+  auto kern = box_mean<Acc>;
+  VSR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  dim3 grid(static_cast<unsigned>((a.W + kBTW - 1) / kBTW), static_cast<unsigned>((a.H + kBTH - 1) / kBTH));
+  if (grid.y > 65535u) return fail(VSR_ERR_UNSUPPORTED, "raster too tall for the focal mean grid");
+  kern<<<grid, 256, smem, st>>>(a);
+  VSR_CUDA_TRY(cudaGetLastError());
+  return VSR_OK;
+}
+
+// ------------------------------------------------------- shared checks --
+int check_raster(const void* src, int dtype, int64_t H, int64_t W, int64_t pitch, const void* dst,
+                 int out_dtype, int64_t out_pitch) {
+  if (H < 0 || W < 0) return fail(VSR_ERR_INVALID_ARG, "negative raster size");
+  if (H == 0 || W == 0) return VSR_OK;
+  if (!src || !dst) return fail(VSR_ERR_INVALID_ARG, "src/dst must not be NULL");
+  if (dtype_size(dtype) == 0) return fail(VSR_ERR_INVALID_ARG, "unsupported dtype %d", dtype);
+  if (out_dtype != VSR_F32 && out_dtype != VSR_F64) return fail(VSR_ERR_INVALID_ARG, "out_dtype must be VSR_F32 or VSR_F64");
+  if (pitch < W || out_pitch < W) return fail(VSR_ERR_INVALID_ARG, "pitch smaller than width");
+  if (!aligned(src, dtype_size(dtype)) || !aligned(dst, out_dtype == VSR_F64 ? 8 : 4))
+    return fail(VSR_ERR_INVALID_ARG, "src/dst not aligned to their element size");
+  return VSR_OK;
+}
+
+}  // namespace
+
+// Workspace layout for the plain FP32 convolution:
+//   [0, 8 kh kw)                  float64 weights (copied from the host)
+//   [256-aligned) kh x kw4 float  float32 weight rows
+//   [+256-aligned) 1 float        total weight
+size_t conv_ws_plain(int kh, int kw) {
+  const size_t a = (static_cast<size_t>(kh) * kw * 8 + 255) & ~size_t(255);
+  const size_t b = (static_cast<size_t>(kh) * ((kw + 3) & ~3) * 4 + 255) & ~size_t(255);
+  return a + b + 256;
+}
+
+}  // namespace vsr
+
+using namespace vsr;
 
 extern "C" size_t vsr_convolve_workspace_size(int kh, int kw, int precision) {
   (void)precision;
   if (kh <= 0 || kw <= 0) return 0;
-  return (static_cast<size_t>(kh) * kw * 8 + 255) & ~size_t(255);
+  return conv_ws_plain(kh, kw);
 }
 
-extern "C" int vsr_convolve(const void*, int, int64_t, int64_t, int64_t, const double*, int, int,
-                            double, int, void*, int, int64_t, int, void*, size_t, void*) {
-  return vsr::fail(VSR_ERR_UNSUPPORTED, "vsr_convolve not built yet");
+extern "C" int vsr_convolve(const void* src, int dtype, int64_t height, int64_t width, int64_t pitch,
+                            const double* weights_host, int kh, int kw, double nodata, int nodata_kind,
+                            void* dst, int out_dtype, int64_t out_pitch, int precision, void* workspace,
+                            size_t workspace_bytes, void* stream) {
+  int rc = check_raster(src, dtype, height, width, pitch, dst, out_dtype, out_pitch);
+  if (rc || height == 0 || width == 0) return rc;
+  if (!weights_host) return fail(VSR_ERR_INVALID_ARG, "weights_host is NULL");
+  if (kh <= 0 || kw <= 0) return fail(VSR_ERR_INVALID_ARG, "kernel must be at least 1 x 1");
+  if (precision < VSR_PREC_AUTO || precision > VSR_PREC_SPLIT_BF16) return fail(VSR_ERR_INVALID_ARG, "bad precision %d", precision);
+  if (kh > kMaxDirectK || kw > kMaxDirectK)
+    return fail(VSR_ERR_UNSUPPORTED, "kernel %dx%d larger than the supported %dx%d", kh, kw, kMaxDirectK, kMaxDirectK);
+  if (precision == VSR_PREC_SPLIT_BF16) return fail(VSR_ERR_UNSUPPORTED, "split-BF16 convolution not in this build");
+  const size_t need = conv_ws_plain(kh, kw);
+  if (!workspace || workspace_bytes < need || !aligned(workspace, 256))
+    return fail(VSR_ERR_WORKSPACE, "workspace must be 256-byte aligned and >= %zu bytes", need);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  char* ws = static_cast<char*>(workspace);
+  double* w64 = reinterpret_cast<double*>(ws);
+  float* w32 = reinterpret_cast<float*>(ws + ((static_cast<size_t>(kh) * kw * 8 + 255) & ~size_t(255)));
+  float* wsum = reinterpret_cast<float*>(ws + need - 256);
+  const int kw4 = (kw + 3) & ~3;
+  VSR_CUDA_TRY(cudaMemcpyAsync(w64, weights_host, static_cast<size_t>(kh) * kw * 8, cudaMemcpyHostToDevice, st));
+  prep_weights<<<1, 256, 0, st>>>(w64, kh, kw, kw4, w32, wsum);
+  VSR_CUDA_TRY(cudaGetLastError());
+  ConvArgs a{src, dtype, height, width, pitch, make_nodata(dtype, nodata, nodata_kind), w32, wsum, kh, kw, kw4,
+             nodata, dst, out_dtype, out_pitch};
+  return run_conv_direct(a, st);
+}
+
+// Gaussian workspace: g (k4 floats) | dense weights (k x k4 floats) | total.
+static size_t gauss_ws(int k) {
+  const int k4 = (k + 3) & ~3;
+  const size_t a = (static_cast<size_t>(k4) * 4 + 255) & ~size_t(255);
+  const size_t b = (static_cast<size_t>(k) * k4 * 4 + 255) & ~size_t(255);
+  return a + b + 256;
+}
+
+static int gaussian_size(double sigma, int kernel_size) {
+  int k = kernel_size > 0 ? kernel_size : static_cast<int>(2.0 * std::ceil(3.0 * sigma) + 1.0);
+  if (k % 2 == 0) k += 1;
+  return k;
 }
 
 extern "C" size_t vsr_gaussian_workspace_size(int kernel_size, int precision) {
   (void)precision;
-  return (static_cast<size_t>(kernel_size > 0 ? kernel_size : 1) * 16 + 255) & ~size_t(255);
+  if (kernel_size <= 0) return 0;
+  const int k = kernel_size % 2 == 0 ? kernel_size + 1 : kernel_size;
+  return gauss_ws(k);
 }
 
-extern "C" int vsr_gaussian(const void*, int, int64_t, int64_t, int64_t, double, int, double, int,
-                            void*, int, int64_t, int, void*, size_t, void*) {
-  return vsr::fail(VSR_ERR_UNSUPPORTED, "vsr_gaussian not built yet");
+extern "C" int vsr_gaussian(const void* src, int dtype, int64_t height, int64_t width, int64_t pitch, double sigma,
+                            int kernel_size, double nodata, int nodata_kind, void* dst, int out_dtype,
+                            int64_t out_pitch, int precision, void* workspace, size_t workspace_bytes,
+                            void* stream) {
+  if (!(sigma > 0.0)) return fail(VSR_ERR_INVALID_ARG, "sigma must be positive, got %g", sigma);
+  int rc = check_raster(src, dtype, height, width, pitch, dst, out_dtype, out_pitch);
+  if (rc || height == 0 || width == 0) return rc;
+  if (precision < VSR_PREC_AUTO || precision > VSR_PREC_SPLIT_BF16) return fail(VSR_ERR_INVALID_ARG, "bad precision %d", precision);
+  if (precision == VSR_PREC_SPLIT_BF16) return fail(VSR_ERR_UNSUPPORTED, "split-BF16 Gaussian not in this build");
+  const int k = gaussian_size(sigma, kernel_size);
+  if (k > kMaxDirectK) return fail(VSR_ERR_UNSUPPORTED, "Gaussian kernel %d larger than %d", k, kMaxDirectK);
+  const size_t need = gauss_ws(k);
+  if (!workspace || workspace_bytes < need || !aligned(workspace, 256))
+    return fail(VSR_ERR_WORKSPACE, "workspace must be 256-byte aligned and >= %zu bytes", need);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int k4 = (k + 3) & ~3;
+  char* ws = static_cast<char*>(workspace);
+  float* g32 = reinterpret_cast<float*>(ws);
+  float* w2 = reinterpret_cast<float*>(ws + ((static_cast<size_t>(k4) * 4 + 255) & ~size_t(255)));
+  float* wsum = reinterpret_cast<float*>(ws + need - 256);
+  const bool separable = k <= kMaxSepK;
+  prep_gaussian<<<1, 256, k * sizeof(double), st>>>(k, k4, sigma, g32, separable ? nullptr : w2, wsum);
+  VSR_CUDA_TRY(cudaGetLastError());
+  const NodataSpec nd = make_nodata(dtype, nodata, nodata_kind);
+  if (separable) {
+    SepArgs a{src, dtype, height, width, pitch, nd, g32, k, nodata, dst, out_dtype, out_pitch};
+    if (k <= 8) return launch_sep<8>(a, st);
+    if (k <= 16) return launch_sep<16>(a, st);
+    return launch_sep<33>(a, st);
+  }
+  ConvArgs a{src, dtype, height, width, pitch, nd, w2, wsum, k, k, k4, nodata, dst, out_dtype, out_pitch};
+  return run_conv_direct(a, st);
 }
 
-extern "C" int vsr_focal_mean(const void*, int, int64_t, int64_t, int64_t, int, int, double, int,
-                              void*, int, int64_t, void*) {
-  return vsr::fail(VSR_ERR_UNSUPPORTED, "vsr_focal_mean not built yet");
+extern "C" int vsr_focal_mean(const void* src, int dtype, int64_t height, int64_t width, int64_t pitch,
+                              int radius_y, int radius_x, double nodata, int nodata_kind, void* dst, int out_dtype,
+                              int64_t out_pitch, void* stream) {
+  int rc = check_raster(src, dtype, height, width, pitch, dst, out_dtype, out_pitch);
+  if (rc || height == 0 || width == 0) return rc;
+  if (radius_y < 0 || radius_x < 0) return fail(VSR_ERR_INVALID_ARG, "radius must be non-negative");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  BoxArgs a{src, dtype, height, width, pitch, make_nodata(dtype, nodata, nodata_kind), radius_y, radius_x,
+            nodata, dst, out_dtype, out_pitch};
+  switch (dtype) {
+    case VSR_U8:
+    case VSR_I16:
+    case VSR_U16: return launch_box<AccI>(a, st);
+    case VSR_F32: return launch_box<AccF2>(a, st);
+    default: return launch_box<AccD>(a, st);
+  }
 }

@@ -11,6 +11,9 @@ __version__ = "0.1.0"
 from vsr_gb300._lib import load as load_library  # noqa: F401
 from vsr_gb300.algebra import (  # noqa: F401
     raster_aspect,
+    raster_convolve,
+    raster_focal_mean,
+    raster_gaussian_filter,
     raster_hillshade,
     raster_slope,
     raster_terrain,
@@ -36,6 +39,9 @@ __all__ = [
     "from_numpy",
     "load_library",
     "raster_aspect",
+    "raster_convolve",
+    "raster_focal_mean",
+    "raster_gaussian_filter",
     "raster_hillshade",
     "raster_slope",
     "raster_terrain",
