@@ -200,6 +200,9 @@ def run_vsr(args, ws, rank, local):
     def step():
         algebra.horn_fused(r, out=outs)
 
+    from vsr_gb300 import autotune
+
+    tuned = autotune.autotune_horn(r, outputs=outs)
     for _ in range(max(3, args.warmup)):
         step()
     torch.cuda.synchronize()
@@ -284,7 +287,10 @@ def run_vsr(args, ws, rank, local):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD if H == 16384 else WORKLOAD.replace("16384x16384", f"{H}x{W}"), "pixels": px, "bytes_per_pixel": BYTES_PER_PX,
                        "l2": "inputs+outputs (3.5 GB/step) exceed L2; no flush",
-                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+                       "autotuned": {"rows_per_tile": tuned["shape"][0], "tma_stages": tuned["shape"][1],
+                                     "threads_per_cta": tuned["shape"][2],
+                                     "ms_by_config": {str(k): round(v, 4) for k, v in tuned["ms"].items()}}},
             "gpu_launches": args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,

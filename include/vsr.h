@@ -83,6 +83,20 @@ VSR_API int vsr_device_info(int* sm_count, int* cc_major, int* cc_minor);
  * kernels set when a bounded wait ran out (0 = none).  Synchronises. */
 VSR_API int vsr_poll_device_error(void* stream, uint32_t* code);
 
+/* ---- launch-configuration tuning ----------------------------------------
+ * Tunable operations have a small table of launch configurations (tile
+ * shape, halo staging depth, threads per CTA).  The autotuner
+ * (vsr_gb300.autotune) times them on the caller's own data and stores the
+ * winner with vsr_tuning_set; the choice is process-wide.  No counterpart in
+ * the reference, whose launches use one fixed 16 x 16 block
+ * (algebra.py:2323-2338). */
+#define VSR_OP_HORN 1
+#define VSR_OP_BATCH 2
+#define VSR_OP_COUNT 4
+VSR_API int vsr_tuning_count(int op);              /* configurations of ``op``; 0 if none */
+VSR_API int vsr_tuning_set(int op, int config);
+VSR_API int vsr_tuning_get(int op);
+
 /* ---- Horn 3x3: slope / aspect / hillshade in one pass -------------------
  * Replaces the launches of ``slope_aspect`` (algebra.py:2372-2377, kernel
  * kernels/focal.py:173-283) and ``hillshade`` (algebra.py:2748-2754, kernel

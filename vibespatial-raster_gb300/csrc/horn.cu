@@ -38,8 +38,8 @@ struct HornParams {
   int64_t height, width;
   int64_t in_pitch, out_pitch, hs_pitch;
   float inv8cx, inv8cy;  // 1 / (8 cell) from FP64
-  float zf;
-  float cos_z, sin_z, cos_az, sin_az;
+  float zf, zf2;
+  float cos_z, hs_a, hs_b;  // cos(zen); sin(zen) cos(az) zf; sin(zen) sin(az) zf
   float nd_out_f;   // nodata written to float slope/aspect
   double nd_out_d;  // nodata written to double slope/aspect
   uint32_t flags;
@@ -66,71 +66,74 @@ struct PixelOut {
   uint8_t hs;
 };
 
-// Degree-valued arctangent: t * P(t^2) on t in [0, 1], P a degree-8 minimax
-// polynomial fitted by csrc/fit_atan.py (max error 3.3e-7 deg in float64,
-// 5.3e-6 deg evaluated in float32).  Reduction by octant keeps the axes
-// exact: atan2_deg(+-y, 0) = +-90, atan2_deg(0, -x) = 180.
+// Degree-valued arctangent on t in [0, 1]: t * P(t^2), P the degree-7
+// minimax polynomial fitted by csrc/fit_atan.py (max error 2.1e-6 deg in
+// float64, 7.6e-6 deg evaluated in float32).
 __device__ __forceinline__ float atan_poly_deg(float t) {
   const float u = t * t;
-  float p = 0.14075983191003316f;
-  p = fmaf(p, u, -0.82513653006899812f);
-  p = fmaf(p, u, 2.2792953508350795f);
-  p = fmaf(p, u, -4.1452671300469577f);
-  p = fmaf(p, u, 6.0154525769063225f);
-  p = fmaf(p, u, -8.1137865295205867f);
-  p = fmaf(p, u, 11.451081054241243f);
-  p = fmaf(p, u, -19.09817129772475f);
-  p = fmaf(p, u, 57.29577300327405f);
+  float p = -0.232309317f;
+  p = fmaf(p, u, 1.2526542f);
+  p = fmaf(p, u, -3.20353885f);
+  p = fmaf(p, u, 5.52457099f);
+  p = fmaf(p, u, -7.96905727f);
+  p = fmaf(p, u, 11.4285402f);
+  p = fmaf(p, u, -19.0966035f);
+  p = fmaf(p, u, 57.2957414f);
   return t * p;
 }
 
-// atan2(y, x) in degrees, (-180, 180]; NaN in -> NaN out.
-__device__ __forceinline__ float atan2_deg(float y, float x) {
-  const float ay = fabsf(y), ax = fabsf(x);
-  const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
-  const float t = mx > 0.0f ? __fdividef(mn, mx) : 0.0f;
-  float a = atan_poly_deg(t);
-  if (ay > ax) a = 90.0f - a;
-  if (signbit(x)) a = 180.0f - a;
-  a = copysignf(a, y);
-  const float nan_probe = x + y;
-  return nan_probe != nan_probe ? nan_probe : a;
-}
-
-// atan(sqrt(s)) in degrees for s = p^2 + q^2 >= 0 (NaN propagates).
-__device__ __forceinline__ float slope_deg_from_sq(float s) {
-  const float r = s > 0.0f ? s * rsqrtf(s) : s;
-  const bool big = r > 1.0f;
-  const float t = big ? __frcp_rn(r) : r;
+// Slope in degrees from s = p^2 + q^2: atan(r), r = sqrt(s), reduced to
+// t = min(r, 1/r) with one rsqrt (r = s * rsqrt(s), 1/r = rsqrt(s)).
+// s = 0 gives exactly 0; NaN propagates.
+__device__ __forceinline__ float slope_deg(float s) {
+  const float rs = rsqrtf(fmaxf(s, 1e-30f));
+  const bool big = s > 1.0f;
+  const float t = big ? rs : s * rs;
   const float a = atan_poly_deg(t);
   return big ? 90.0f - a : a;
 }
 
-// gx, gy: raw Horn sums (before the 1/(8 cell) scale).
+// Aspect in compass degrees: (90 - atan2(-q, p) in degrees) mod 360.  The
+// octant reduction keeps the axes exact (due north 0, east 90, south 180,
+// west 270, flat 90 as atan2(-0, +0) = -0 gives); NaN propagates.
+__device__ __forceinline__ float aspect_deg(float p, float q) {
+  const float ap = fabsf(p), aq = fabsf(q);
+  const float mx = fmaxf(ap, aq), mn = fminf(ap, aq);
+  const float t = __fdividef(mn, fmaxf(mx, 1e-30f));
+  float a = atan_poly_deg(t);
+  a = aq > ap ? 90.0f - a : a;      // |atan2| folded into [0, 90]
+  a = p < 0.0f ? 180.0f - a : a;    // [0, 180]
+  // atan2(-q, p) = +a for q <= 0, -a for q > 0; aspect = 90 - atan2
+  float asp = q > 0.0f ? 90.0f + a : 90.0f - a;
+  asp = asp < 0.0f ? asp + 360.0f : asp;
+  const float nan_probe = p * q;
+  return nan_probe != nan_probe ? nan_probe : asp;
+}
+
+// Hillshade byte from the unscaled gradient (p, q) and s = p^2 + q^2:
+// (cos zen + sin zen (cos az p' - sin az q')) / sqrt(1 + p'^2 + q'^2) with
+// p' = zf p, q' = zf q, saturated to [0, 1] (NaN -> 0), uint8(hs*255 + 0.5).
+__device__ __forceinline__ uint8_t hillshade_u8(float p, float q, float s, const HornParams& P) {
+  const float num = fmaf(P.hs_a, p, fmaf(-P.hs_b, q, P.cos_z));
+  const float hs = __saturatef(num * rsqrtf(fmaf(P.zf2, s, 1.0f)));
+  return static_cast<uint8_t>(__float2uint_rz(fmaf(hs, 255.0f, 0.5f)));
+}
+
 __device__ __forceinline__ PixelOut horn_pixel(float gx, float gy, const HornParams& P, bool want_s,
                                                bool want_a, bool want_h) {
   PixelOut o;
   const float p = gx * P.inv8cx;
   const float q = gy * P.inv8cy;
-  if (want_s) o.slope = slope_deg_from_sq(p * p + q * q);
-  if (want_a) {
-    const float t = 90.0f - atan2_deg(-q, p);
-    o.aspect = t < 0.0f ? t + 360.0f : t;
-  }
-  if (want_h) {
-    const float ph = p * P.zf, qh = q * P.zf;
-    const float num = P.cos_z + P.sin_z * (P.cos_az * ph - P.sin_az * qh);
-    float hs = num * rsqrtf(1.0f + ph * ph + qh * qh);
-    hs = fminf(fmaxf(hs, 0.0f), 1.0f);  // NaN -> 0
-    o.hs = static_cast<uint8_t>(__float2uint_rz(hs * 255.0f + 0.5f));
-  }
+  const float s = fmaf(p, p, q * q);
+  if (want_s) o.slope = slope_deg(s);
+  if (want_a) o.aspect = aspect_deg(p, q);
+  if (want_h) o.hs = hillshade_u8(p, q, s, P);
   return o;
 }
 
 // ------------------------------------------------------------ TMA kernel --
 constexpr int kTW = 128;        // output tile width (32 lanes x 4 pixels)
 constexpr int kSW = kTW + 8;    // staged width: 4-column halo each side (16 B)
-constexpr int kThreads = 256;
 
 template <int TH>
 struct TmaTile {
@@ -149,25 +152,124 @@ __device__ __forceinline__ void load6(const float* row, int lane, float v[6]) {
   v[5] = row[8 + 4 * lane];
 }
 
+__device__ __forceinline__ bool is_nd(float v, int kind, float ndv) {
+  return kind == VSR_NODATA_VALUE ? (v == ndv) : (kind == VSR_NODATA_NAN ? (v != v) : false);
+}
+
 __device__ __forceinline__ uint32_t nd_bits6(const float v[6], int kind, float ndv) {
   uint32_t m = 0;
 #pragma unroll
-  for (int k = 0; k < 6; ++k) {
-    const bool b = (kind == VSR_NODATA_VALUE) ? (v[k] == ndv) : (kind == VSR_NODATA_NAN ? (v[k] != v[k]) : false);
-    m |= (b ? 1u : 0u) << k;
-  }
+  for (int k = 0; k < 6; ++k) m |= (is_nd(v[k], kind, ndv) ? 1u : 0u) << k;
   return m;
 }
 
-template <int TH, int STAGES>
-__global__ void __launch_bounds__(kThreads) horn_f32_tma(const __grid_constant__ CUtensorMap tmap,
-                                                         const HornParams P, const float nd_in,
-                                                         float* __restrict__ slope,
-                                                         float* __restrict__ aspect,
-                                                         uint8_t* __restrict__ hs,
-                                                         uint32_t* err_word) {
+// RB output rows of one warp: rows r0 .. r0+RB-1 of the tile (staged rows
+// r0 .. r0+RB+1), lane columns xs .. xs+3.  Horizontal differences of a staged
+// row are formed once and reused by the three output rows that need them.
+template <int RB, bool MASKED>
+__device__ __forceinline__ void horn_rows(const float* S, int lane, int r0, int64_t y0, int64_t xs,
+                                          const HornParams& P, const MaskRule& rule, float nd_in,
+                                          float* __restrict__ slope, float* __restrict__ aspect,
+                                          uint8_t* __restrict__ hs) {
+  const int64_t W = P.width, H = P.height;
+  const bool want_s = slope != nullptr, want_a = aspect != nullptr, want_h = hs != nullptr;
+  float top[6], mid[6], bot[6];
+  float hdt[4], hdm[4], hdb[4];
+  load6(S + (r0 + 0) * kSW, lane, top);
+  load6(S + (r0 + 1) * kSW, lane, mid);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    hdt[k] = top[k + 2] - top[k];
+    hdm[k] = mid[k + 2] - mid[k];
+  }
+  uint32_t mt = 0, mm = 0;
+  if (MASKED) {
+    mt = nd_bits6(top, P.nd_kind, nd_in);
+    mm = nd_bits6(mid, P.nd_kind, nd_in);
+  }
+#pragma unroll
+  for (int j = 0; j < RB; ++j) {
+    load6(S + (r0 + j + 2) * kSW, lane, bot);
+    float dv[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) dv[k] = bot[k] - top[k];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) hdb[k] = bot[k + 2] - bot[k];
+    uint32_t mb = 0;
+    if (MASKED) mb = nd_bits6(bot, P.nd_kind, nd_in);
+    const int64_t y = y0 + r0 + j;
+    if (y < H && xs < W) {
+      uint32_t hdil = 0, ctr = 0;
+      if (MASKED) {
+        hdil = (mt | (mt >> 1) | (mt >> 2)) | (mm | (mm >> 1) | (mm >> 2)) | (mb | (mb >> 1) | (mb >> 2));
+        ctr = mm >> 1;
+      }
+      float so[4], ao[4];
+      uint8_t ho[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float gx = fmaf(2.0f, hdm[k], hdt[k] + hdb[k]);
+        const float gy = fmaf(2.0f, dv[k + 1], dv[k] + dv[k + 2]);
+        const PixelOut o = horn_pixel(gx, gy, P, want_s, want_a, want_h);
+        so[k] = o.slope;
+        ao[k] = o.aspect;
+        ho[k] = o.hs;
+        if (MASKED) {
+          const bool sa_nd = rule.sa_any && (((rule.sa_center ? ctr : hdil) >> k) & 1u);
+          const bool hs_nd = rule.hs_any && ((hdil >> k) & 1u);
+          so[k] = sa_nd ? P.nd_out_f : so[k];
+          ao[k] = sa_nd ? P.nd_out_f : ao[k];
+          ho[k] = hs_nd ? uint8_t(0) : ho[k];
+        }
+      }
+      const bool full = xs + 3 < W;
+      if (want_s) {
+        float* dst = slope + y * P.out_pitch + xs;
+        if (full) __stcs(reinterpret_cast<float4*>(dst), make_float4(so[0], so[1], so[2], so[3]));
+        else for (int k = 0; k < 4; ++k) if (xs + k < W) __stcs(dst + k, so[k]);
+      }
+      if (want_a) {
+        float* dst = aspect + y * P.out_pitch + xs;
+        if (full) __stcs(reinterpret_cast<float4*>(dst), make_float4(ao[0], ao[1], ao[2], ao[3]));
+        else for (int k = 0; k < 4; ++k) if (xs + k < W) __stcs(dst + k, ao[k]);
+      }
+      if (want_h) {
+        uint8_t* dst = hs + y * P.hs_pitch + xs;
+        if (full) {
+          const uint32_t packed = uint32_t(ho[0]) | (uint32_t(ho[1]) << 8) | (uint32_t(ho[2]) << 16) |
+                                  (uint32_t(ho[3]) << 24);
+          __stcs(reinterpret_cast<unsigned int*>(dst), packed);
+        } else {
+          for (int k = 0; k < 4; ++k) if (xs + k < W) dst[k] = ho[k];
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      top[k] = mid[k];
+      mid[k] = bot[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      hdt[k] = hdm[k];
+      hdm[k] = hdb[k];
+    }
+    mt = mm;
+    mm = mb;
+  }
+}
+
+template <int TH, int STAGES, int THREADS>
+__global__ void __launch_bounds__(THREADS) horn_f32_tma(const __grid_constant__ CUtensorMap tmap,
+                                                        const HornParams P, const float nd_in,
+                                                        float* __restrict__ slope,
+                                                        float* __restrict__ aspect,
+                                                        uint8_t* __restrict__ hs,
+                                                        uint32_t* err_word) {
   using Tile = TmaTile<TH>;
-  constexpr int RB = TH / (kThreads / 32);  // rows per warp
+  constexpr int WARPS = THREADS / 32;
+  constexpr int RB = TH / WARPS;  // output rows per warp
+  static_assert(RB * WARPS == TH, "TH must be a multiple of the warp count");
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bars[STAGES];
   float* stages = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -177,7 +279,6 @@ __global__ void __launch_bounds__(kThreads) horn_f32_tma(const __grid_constant__
   const int64_t tiles_x = (W + kTW - 1) / kTW;
   const int64_t total = tiles_x * ((H + TH - 1) / TH);
   const MaskRule rule = mask_rule(P);
-  const bool want_s = slope != nullptr, want_a = aspect != nullptr, want_h = hs != nullptr;
 
   auto issue = [&](int64_t t, int s) {
     const int64_t ty = t / tiles_x, tx = t - ty * tiles_x;
@@ -226,7 +327,7 @@ __global__ void __launch_bounds__(kThreads) horn_f32_tma(const __grid_constant__
     const bool left = x0 == 0, right = x0 + kTW >= W, top = y0 == 0, bottom = y0 + TH >= H;
     if (left || right) {
       const int rc = static_cast<int>(W - x0) + 4;  // staged column of x = W
-      for (int r = tid; r < Tile::SH; r += kThreads) {
+      for (int r = tid; r < Tile::SH; r += THREADS) {
         if (left) S[r * kSW + 3] = S[r * kSW + 4];
         if (right) S[r * kSW + rc] = S[r * kSW + rc - 1];
       }
@@ -234,73 +335,30 @@ __global__ void __launch_bounds__(kThreads) horn_f32_tma(const __grid_constant__
     if (top || bottom) {
       __syncthreads();
       const int rr = static_cast<int>(H - y0) + 1;  // staged row of y = H
-      for (int c = tid; c < kSW; c += kThreads) {
+      for (int c = tid; c < kSW; c += THREADS) {
         if (top) S[c] = S[kSW + c];
         if (bottom) S[rr * kSW + c] = S[(rr - 1) * kSW + c];
       }
     }
-    __syncthreads();
-
-    // Each warp: RB output rows; each lane: 4 adjacent columns.
-    const int64_t xs = x0 + 4 * lane;
-    const int r0 = warp * RB;
-    float top6[6], mid6[6], bot6[6];
-    load6(S + (r0 + 0) * kSW, lane, top6);
-    load6(S + (r0 + 1) * kSW, lane, mid6);
-    uint32_t mt = nd_bits6(top6, P.nd_kind, nd_in);
-    uint32_t mm = nd_bits6(mid6, P.nd_kind, nd_in);
-#pragma unroll
-    for (int j = 0; j < RB; ++j) {
-      load6(S + (r0 + j + 2) * kSW, lane, bot6);
-      const uint32_t mb = nd_bits6(bot6, P.nd_kind, nd_in);
-      const int64_t y = y0 + r0 + j;
-      if (y < H && xs < W) {
-        const uint32_t hdil = (mt | (mt >> 1) | (mt >> 2)) | (mm | (mm >> 1) | (mm >> 2)) |
-                              (mb | (mb >> 1) | (mb >> 2));
-        const uint32_t ctr = mm >> 1;
-        float so[4], ao[4];
-        uint8_t ho[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const float gx = (top6[k + 2] - top6[k]) + 2.0f * (mid6[k + 2] - mid6[k]) + (bot6[k + 2] - bot6[k]);
-          const float gy = (bot6[k] - top6[k]) + 2.0f * (bot6[k + 1] - top6[k + 1]) + (bot6[k + 2] - top6[k + 2]);
-          PixelOut o = horn_pixel(gx, gy, P, want_s, want_a, want_h);
-          const bool sa_nd = rule.sa_any && (((rule.sa_center ? ctr : hdil) >> k) & 1u);
-          const bool hs_nd = rule.hs_any && ((hdil >> k) & 1u);
-          so[k] = sa_nd ? P.nd_out_f : o.slope;
-          ao[k] = sa_nd ? P.nd_out_f : o.aspect;
-          ho[k] = hs_nd ? uint8_t(0) : o.hs;
-        }
-        const bool full = xs + 3 < W;
-        if (want_s) {
-          float* dst = slope + y * P.out_pitch + xs;
-          if (full) __stcs(reinterpret_cast<float4*>(dst), make_float4(so[0], so[1], so[2], so[3]));
-          else for (int k = 0; k < 4; ++k) if (xs + k < W) __stcs(dst + k, so[k]);
-        }
-        if (want_a) {
-          float* dst = aspect + y * P.out_pitch + xs;
-          if (full) __stcs(reinterpret_cast<float4*>(dst), make_float4(ao[0], ao[1], ao[2], ao[3]));
-          else for (int k = 0; k < 4; ++k) if (xs + k < W) __stcs(dst + k, ao[k]);
-        }
-        if (want_h) {
-          uint8_t* dst = hs + y * P.hs_pitch + xs;
-          if (full) {
-            const uint32_t packed = uint32_t(ho[0]) | (uint32_t(ho[1]) << 8) | (uint32_t(ho[2]) << 16) |
-                                    (uint32_t(ho[3]) << 24);
-            __stcs(reinterpret_cast<unsigned int*>(dst), packed);
-          } else {
-            for (int k = 0; k < 4; ++k) if (xs + k < W) dst[k] = ho[k];
-          }
-        }
+    // Does the staged tile hold any nodata at all?  Clean tiles skip every
+    // mask operation.
+    bool any_nd = false;
+    if (P.nd_kind != VSR_NODATA_NONE) {
+      __syncthreads();
+      const float4* S4 = reinterpret_cast<const float4*>(S);
+      for (int i = tid; i < Tile::SH * kSW / 4; i += THREADS) {
+        const float4 v = S4[i];
+        any_nd |= is_nd(v.x, P.nd_kind, nd_in) | is_nd(v.y, P.nd_kind, nd_in) |
+                  is_nd(v.z, P.nd_kind, nd_in) | is_nd(v.w, P.nd_kind, nd_in);
       }
-#pragma unroll
-      for (int k = 0; k < 6; ++k) {
-        top6[k] = mid6[k];
-        mid6[k] = bot6[k];
-      }
-      mt = mm;
-      mm = mb;
     }
+    const bool masked = __syncthreads_or(any_nd);
+
+    const int64_t xs = x0 + 4 * lane;
+    if (masked)
+      horn_rows<RB, true>(S, lane, warp * RB, y0, xs, P, rule, nd_in, slope, aspect, hs);
+    else
+      horn_rows<RB, false>(S, lane, warp * RB, y0, xs, P, rule, nd_in, slope, aspect, hs);
 
     __syncthreads();  // every read of stage s is done
     if (tid == 0) {
@@ -383,7 +441,7 @@ int dispatch_generic(int dtype, const void* src, const HornParams& P, double ndv
   }
 }
 
-template <int TH, int STAGES>
+template <int TH, int STAGES, int THREADS>
 int launch_tma(const void* src, const HornParams& P, float nd_in, float* slope, float* aspect,
                uint8_t* hs, cudaStream_t st) {
   using Tile = TmaTile<TH>;
@@ -394,25 +452,41 @@ int launch_tma(const void* src, const HornParams& P, float nd_in, float* slope, 
   uint32_t* err = device_error_word();
   if (!err) return VSR_ERR_CUDA;
   const size_t smem = STAGES * Tile::kStride + 1024;
-  auto kern = horn_f32_tma<TH, STAGES>;
-  static bool attr_set[64] = {};
-  int dev = 0;
-  VSR_CUDA_TRY(cudaGetDevice(&dev));
-  if (dev < 64 && !attr_set[dev]) {
-    VSR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-    attr_set[dev] = true;
-  }
+  auto kern = horn_f32_tma<TH, STAGES, THREADS>;
+  VSR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   int per_sm = 0;
-  VSR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem));
+  VSR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, THREADS, smem));
   if (per_sm < 1) return fail(VSR_ERR_CUDA, "horn_f32_tma cannot be resident (smem %zu)", smem);
   const int64_t tiles = ((P.width + kTW - 1) / kTW) * ((P.height + TH - 1) / TH);
   const int64_t grid = std::min<int64_t>(tiles, static_cast<int64_t>(sm_count()) * per_sm);
-  kern<<<static_cast<unsigned>(grid), kThreads, smem, st>>>(map, P, nd_in, slope, aspect, hs, err);
+  kern<<<static_cast<unsigned>(grid), THREADS, smem, st>>>(map, P, nd_in, slope, aspect, hs, err);
   VSR_CUDA_TRY(cudaGetLastError());
   return VSR_OK;
 }
 
+// Launch configurations of the TMA kernel the autotuner chooses between:
+// (output rows per tile, pipeline stages, threads per CTA).
+struct HornConfig {
+  int th, stages, threads;
+};
+constexpr HornConfig kHornConfigs[] = {{32, 3, 256}, {64, 2, 256}, {16, 4, 128}, {32, 2, 128}, {64, 3, 256}};
+constexpr int kNumHornConfigs = sizeof(kHornConfigs) / sizeof(kHornConfigs[0]);
+
+int launch_tma_config(int cfg, const void* src, const HornParams& P, float nd_in, float* slope,
+                      float* aspect, uint8_t* hs, cudaStream_t st) {
+  switch (cfg) {
+    case 1: return launch_tma<64, 2, 256>(src, P, nd_in, slope, aspect, hs, st);
+    case 2: return launch_tma<16, 4, 128>(src, P, nd_in, slope, aspect, hs, st);
+    case 3: return launch_tma<32, 2, 128>(src, P, nd_in, slope, aspect, hs, st);
+    case 4: return launch_tma<64, 3, 256>(src, P, nd_in, slope, aspect, hs, st);
+    default: return launch_tma<32, 3, 256>(src, P, nd_in, slope, aspect, hs, st);
+  }
+}
+
 }  // namespace
+
+int horn_config_count() { return kNumHornConfigs; }
+
 }  // namespace vsr
 
 extern "C" int vsr_horn_fused(const void* dem, int dtype, int64_t height, int64_t width, int64_t pitch,
@@ -450,10 +524,10 @@ extern "C" int vsr_horn_fused(const void* dem, int dtype, int64_t height, int64_
   P.inv8cx = static_cast<float>(1.0 / (8.0 * cell_x));
   P.inv8cy = static_cast<float>(1.0 / (8.0 * cell_y));
   P.zf = static_cast<float>(z_factor);
+  P.zf2 = static_cast<float>(z_factor * z_factor);
   P.cos_z = static_cast<float>(std::cos(zenith_rad));
-  P.sin_z = static_cast<float>(std::sin(zenith_rad));
-  P.cos_az = static_cast<float>(std::cos(azimuth_rad));
-  P.sin_az = static_cast<float>(std::sin(azimuth_rad));
+  P.hs_a = static_cast<float>(std::sin(zenith_rad) * std::cos(azimuth_rad) * z_factor);
+  P.hs_b = static_cast<float>(std::sin(zenith_rad) * std::sin(azimuth_rad) * z_factor);
   P.nd_out_f = static_cast<float>(nodata);
   P.nd_out_d = nodata;
   P.flags = flags;
@@ -467,8 +541,8 @@ extern "C" int vsr_horn_fused(const void* dem, int dtype, int64_t height, int64_
                       (!hillshade || (aligned(hillshade, 4) && hs_pitch % 4 == 0)) &&
                       width < (int64_t(1) << 31) && height < (int64_t(1) << 31);
   if (tma_ok)
-    return launch_tma<32, 3>(dem, P, static_cast<float>(ndv), static_cast<float*>(slope),
-                             static_cast<float*>(aspect), hillshade, st);
+    return launch_tma_config(tuning_get(VSR_OP_HORN), dem, P, static_cast<float>(ndv),
+                             static_cast<float*>(slope), static_cast<float*>(aspect), hillshade, st);
   if ((slope || aspect) && out_dtype == VSR_F64)
     return dispatch_generic<double>(dtype, dem, P, ndv, slope, aspect, hillshade, st);
   return dispatch_generic<float>(dtype, dem, P, ndv, slope, aspect, hillshade, st);

@@ -2,6 +2,7 @@
 // info, the device-side error word and tensor-map encoding.
 #include <cstdarg>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 
 #include "vsr_internal.cuh"
@@ -139,6 +140,11 @@ int encode_tensor_map_2d(CUtensorMap* map, CUtensorMapDataType type, size_t elem
   return VSR_OK;
 }
 
+// Selected launch configuration per tunable operation (process-wide).
+static std::atomic<int> g_tuning[VSR_OP_COUNT];
+
+int tuning_get(int op) { return (op >= 0 && op < VSR_OP_COUNT) ? g_tuning[op].load() : 0; }
+
 }  // namespace vsr
 
 extern "C" {
@@ -155,6 +161,23 @@ int vsr_device_info(int* sm_count, int* cc_major, int* cc_minor) {
   if (cc_minor) VSR_CUDA_TRY(cudaDeviceGetAttribute(cc_minor, cudaDevAttrComputeCapabilityMinor, dev));
   return VSR_OK;
 }
+
+int vsr_tuning_count(int op) {
+  switch (op) {
+    case VSR_OP_HORN: return vsr::horn_config_count();
+    default: return 0;
+  }
+}
+
+int vsr_tuning_set(int op, int config) {
+  const int n = vsr_tuning_count(op);
+  if (n == 0) return vsr::fail(VSR_ERR_INVALID_ARG, "operation %d has no tunable configurations", op);
+  if (config < 0 || config >= n) return vsr::fail(VSR_ERR_INVALID_ARG, "config %d out of range [0, %d)", config, n);
+  vsr::g_tuning[op].store(config);
+  return VSR_OK;
+}
+
+int vsr_tuning_get(int op) { return vsr::tuning_get(op); }
 
 int vsr_poll_device_error(void* stream, uint32_t* code) {
   if (!code) return vsr::fail(VSR_ERR_INVALID_ARG, "code must not be NULL");

@@ -42,6 +42,10 @@ constexpr uint64_t kWaitLimitNs = 2000000000ull;
 
 int sm_count();  // cached per device
 
+// Launch-configuration table chosen by the autotuner (vsr_tuning_set).
+int tuning_get(int op);
+int horn_config_count();
+
 // ----------------------------------------------------------- dtype traits --
 inline size_t dtype_size(int dt) {
   switch (dt) {

@@ -26,6 +26,7 @@ VSR_NODATA_NONE, VSR_NODATA_VALUE, VSR_NODATA_NAN = 0, 1, 2
 VSR_HORN_CENTER_ONLY = 1
 VSR_HORN_SA_NAN_UNMASKED = 2
 VSR_PREC_AUTO, VSR_PREC_FP32, VSR_PREC_SPLIT_BF16 = 0, 1, 2
+VSR_OP_HORN, VSR_OP_BATCH = 1, 2
 
 DTYPE_CODES = {
     np.dtype(np.uint8): VSR_U8,
@@ -50,6 +51,9 @@ SIGNATURES: dict[str, tuple] = {
     "vsr_last_error": (_c.c_char_p, []),
     "vsr_device_info": (_int, [_c.POINTER(_int), _c.POINTER(_int), _c.POINTER(_int)]),
     "vsr_poll_device_error": (_int, [_vp, _c.POINTER(_u32)]),
+    "vsr_tuning_count": (_int, [_int]),
+    "vsr_tuning_set": (_int, [_int, _int]),
+    "vsr_tuning_get": (_int, [_int]),
     "vsr_horn_fused": (
         _int,
         [_vp, _int, _i64, _i64, _i64, _dbl, _dbl, _dbl, _int, _u32, _vp, _vp, _int, _i64, _vp, _i64,
