@@ -259,11 +259,9 @@ def run_vsr(args, ws, rank, local):
     clocks = sampler.stop()
 
     # max over ranks
-    t_step = ms / args.steps
-    if ws > 1:
-        tt = torch.tensor([t_step, e2e_s], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_step, e2e_s = float(tt[0]), float(tt[1])
+    from vsr_gb300 import replicas
+
+    t_step, e2e_s = replicas.max_over_ranks([ms / args.steps, e2e_s], device=dev)
     value = ws * px / (t_step * 1e-3) / 1e9
     e2e_value = ws * px / e2e_s / 1e9
 

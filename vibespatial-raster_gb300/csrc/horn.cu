@@ -82,11 +82,23 @@ __device__ __forceinline__ float atan_poly_deg(float t) {
   return t * p;
 }
 
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // Slope in degrees from s = p^2 + q^2: atan(r), r = sqrt(s), reduced to
 // t = min(r, 1/r) with one rsqrt (r = s * rsqrt(s), 1/r = rsqrt(s)).
-// s = 0 gives exactly 0; NaN propagates.
+// s = 0 gives exactly 0; NaN propagates (the select keeps s * rsqrt).
 __device__ __forceinline__ float slope_deg(float s) {
-  const float rs = rsqrtf(fmaxf(s, 1e-30f));
+  const float rs = rsqrt_approx(s + 1e-30f);
   const bool big = s > 1.0f;
   const float t = big ? rs : s * rs;
   const float a = atan_poly_deg(t);
@@ -95,19 +107,19 @@ __device__ __forceinline__ float slope_deg(float s) {
 
 // Aspect in compass degrees: (90 - atan2(-q, p) in degrees) mod 360.  The
 // octant reduction keeps the axes exact (due north 0, east 90, south 180,
-// west 270, flat 90 as atan2(-0, +0) = -0 gives); NaN propagates.
+// west 270, flat 90 as atan2(-0, +0) = -0 gives).  The min/max are selects
+// on a comparison, so a NaN operand lands in t and propagates to the result.
 __device__ __forceinline__ float aspect_deg(float p, float q) {
   const float ap = fabsf(p), aq = fabsf(q);
-  const float mx = fmaxf(ap, aq), mn = fminf(ap, aq);
-  const float t = __fdividef(mn, fmaxf(mx, 1e-30f));
+  const bool sw = aq > ap;
+  const float mx = sw ? aq : ap, mn = sw ? ap : aq;
+  const float t = mn * rcp_approx(mx + 1e-30f);
   float a = atan_poly_deg(t);
-  a = aq > ap ? 90.0f - a : a;      // |atan2| folded into [0, 90]
+  a = sw ? 90.0f - a : a;           // |atan2| folded into [0, 90]
   a = p < 0.0f ? 180.0f - a : a;    // [0, 180]
   // atan2(-q, p) = +a for q <= 0, -a for q > 0; aspect = 90 - atan2
-  float asp = q > 0.0f ? 90.0f + a : 90.0f - a;
-  asp = asp < 0.0f ? asp + 360.0f : asp;
-  const float nan_probe = p * q;
-  return nan_probe != nan_probe ? nan_probe : asp;
+  float asp = fmaf(q > 0.0f ? 1.0f : -1.0f, a, 90.0f);
+  return asp < 0.0f ? asp + 360.0f : asp;
 }
 
 // Hillshade byte from the unscaled gradient (p, q) and s = p^2 + q^2:
@@ -115,7 +127,7 @@ __device__ __forceinline__ float aspect_deg(float p, float q) {
 // p' = zf p, q' = zf q, saturated to [0, 1] (NaN -> 0), uint8(hs*255 + 0.5).
 __device__ __forceinline__ uint8_t hillshade_u8(float p, float q, float s, const HornParams& P) {
   const float num = fmaf(P.hs_a, p, fmaf(-P.hs_b, q, P.cos_z));
-  const float hs = __saturatef(num * rsqrtf(fmaf(P.zf2, s, 1.0f)));
+  const float hs = __saturatef(num * rsqrt_approx(fmaf(P.zf2, s, 1.0f)));
   return static_cast<uint8_t>(__float2uint_rz(fmaf(hs, 255.0f, 0.5f)));
 }
 
@@ -187,7 +199,9 @@ __device__ __forceinline__ void horn_rows(const float* S, int lane, int r0, int6
     mt = nd_bits6(top, P.nd_kind, nd_in);
     mm = nd_bits6(mid, P.nd_kind, nd_in);
   }
-#pragma unroll
+  // Rolled on purpose: a fully unrolled row loop overflows the instruction
+  // cache (ncu: "no instruction" stalls dominated).
+#pragma unroll 1
   for (int j = 0; j < RB; ++j) {
     load6(S + (r0 + j + 2) * kSW, lane, bot);
     float dv[6];
