@@ -145,6 +145,25 @@ VSR_API int vsr_convolve(const void* src, int dtype, int64_t height, int64_t wid
                  void* dst, int out_dtype, int64_t out_pitch, int precision, void* workspace,
                  size_t workspace_bytes, void* stream);
 
+/* ---- normalised focal convolution that allocates nothing -----------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory and cannot pass a workspace: a serving process whose device budget
+ * was fixed at start-up, a host that reaches this library through a plugin
+ * boundary (ctypes / cgo / JNI) without the process allocator, or work issued
+ * while a CUDA graph capture forbids allocation.  Same arguments and results
+ * as vsr_convolve without the workspace: the scratch is a static device
+ * array inside libvsr (77,056 bytes, enough for kernels up to 80 x 80,
+ * held by every GPU that loads the library until the process exits).
+ * Kernels larger than 80 x 80 are rejected with VSR_ERR_UNSUPPORTED.  The
+ * first call on each device resolves the array's device address (with that
+ * device current), so make it before any stream capture.  All calls share
+ * the array and it keeps the last call's contents; calls whose kernels
+ * overlap on the GPU (e.g. on two streams at once) race.  No cudaMalloc,
+ * cudaFree or allocating library routine is called. */
+VSR_API int vsr_convolve_noalloc(const void* src, int dtype, int64_t height, int64_t width, int64_t pitch,
+                         const double* weights_host, int kh, int kw, double nodata, int nodata_kind,
+                         void* dst, int out_dtype, int64_t out_pitch, int precision, void* stream);
+
 /* ---- Gaussian filter -----------------------------------------------------
  * Replaces raster_gaussian_filter (algebra.py:2120-2154): weights built in
  * float64 on the device (g_i = exp(-0.5 (i - k/2)^2 / sigma^2)); the filter is

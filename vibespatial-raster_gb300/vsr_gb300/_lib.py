@@ -65,6 +65,10 @@ SIGNATURES: dict[str, tuple] = {
         [_vp, _int, _i64, _i64, _i64, _c.POINTER(_dbl), _int, _int, _dbl, _int, _vp, _int, _i64, _int,
          _vp, _sz, _vp],
     ),
+    "vsr_convolve_noalloc": (
+        _int,
+        [_vp, _int, _i64, _i64, _i64, _c.POINTER(_dbl), _int, _int, _dbl, _int, _vp, _int, _i64, _int, _vp],
+    ),
     "vsr_gaussian_workspace_size": (_sz, [_int, _int]),
     "vsr_gaussian": (
         _int,
