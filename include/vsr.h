@@ -152,7 +152,7 @@ VSR_API int vsr_convolve(const void* src, int dtype, int64_t height, int64_t wid
  * boundary (ctypes / cgo / JNI) without the process allocator, or work issued
  * while a CUDA graph capture forbids allocation.  Same arguments and results
  * as vsr_convolve without the workspace: the scratch is a static device
- * array inside libvsr (77,056 bytes, enough for kernels up to 80 x 80,
+ * array inside libvsr (108,288 bytes, enough for kernels up to 80 x 80,
  * held by every GPU that loads the library until the process exits).
  * Kernels larger than 80 x 80 are rejected with VSR_ERR_UNSUPPORTED.  The
  * first call on each device resolves the array's device address (with that
@@ -189,6 +189,39 @@ VSR_API int vsr_gaussian(const void* src, int dtype, int64_t height, int64_t wid
 VSR_API int vsr_focal_mean(const void* src, int dtype, int64_t height, int64_t width, int64_t pitch,
                    int radius_y, int radius_x, double nodata, int nodata_kind, void* dst,
                    int out_dtype, int64_t out_pitch, void* stream);
+
+/* ---- batched tiles: one persistent launch ------------------------------------
+ * Many float32 DEM tiles of uneven sizes, each with its own cell size and
+ * nodata, processed by ONE work-queue-scheduled persistent launch: slope and
+ * aspect (Horn, as vsr_horn_fused) and a gauss_k x gauss_k Gaussian (as
+ * vsr_gaussian) per tile.  Replaces the reference's per-raster / per-band
+ * launch loops (dispatch.py:417-506, one launch per band and operation).
+ *
+ * vsr_batch_plan uploads the tile descriptors into ``plan`` (device memory of
+ * vsr_batch_plan_size(n) bytes, 256-byte aligned), builds the Gaussian taps in
+ * float64 on the device and synchronises ``stream``.  vsr_batch_run resets the
+ * work counter and launches; it makes no host synchronisation and no
+ * allocation, so it can be captured in a CUDA graph and replayed.  The plan
+ * keeps the tile pointers: replays read and write the same buffers.  The
+ * block shape comes from the tuning table (VSR_OP_BATCH); re-plan after
+ * changing it. */
+typedef struct vsr_batch_tile {
+  const float* src;           /* height x width float32, row pitch ``pitch`` */
+  int64_t height, width, pitch;
+  float* slope;               /* NULL, or with ``aspect``: degrees          */
+  float* aspect;
+  float* smooth;              /* NULL or the Gaussian output                 */
+  int64_t out_pitch;          /* row pitch of the outputs                    */
+  double cell_x, cell_y;      /* |affine a|, |affine e| (1.0 where zero)     */
+  double nodata;
+  int32_t nodata_kind;        /* VSR_NODATA_*                                */
+  uint32_t flags;             /* VSR_HORN_* bits                             */
+} vsr_batch_tile;
+
+VSR_API size_t vsr_batch_plan_size(int n_tiles);
+VSR_API int vsr_batch_plan(const vsr_batch_tile* tiles_host, int n_tiles, double sigma, int gauss_k, void* plan,
+                   size_t plan_bytes, int64_t* total_items, void* stream);
+VSR_API int vsr_batch_run(void* plan, int gauss_k, void* stream);
 
 #ifdef __cplusplus
 }

@@ -591,10 +591,19 @@ size_t conv_ws_plain(int kh, int kw) {
 
 using namespace vsr;
 
+namespace vsr {
+size_t conv_tc_workspace(int kh, int kw);  // conv_tc.cu
+int conv_tc_supported(int kh, int kw);
+int run_conv_tc(const void* src, int dtype, int64_t H, int64_t W, int64_t pitch, const double* weights_host,
+                int kh, int kw, double nodata, int nodata_kind, void* dst, int out_dtype, int64_t out_pitch,
+                void* workspace, size_t ws_bytes, cudaStream_t st);
+}  // namespace vsr
+
 extern "C" size_t vsr_convolve_workspace_size(int kh, int kw, int precision) {
-  (void)precision;
   if (kh <= 0 || kw <= 0) return 0;
-  return conv_ws_plain(kh, kw);
+  size_t n = conv_ws_plain(kh, kw);
+  if (precision != VSR_PREC_FP32 && conv_tc_supported(kh, kw)) n = std::max(n, conv_tc_workspace(kh, kw));
+  return n;
 }
 
 extern "C" int vsr_convolve(const void* src, int dtype, int64_t height, int64_t width, int64_t pitch,
@@ -608,7 +617,15 @@ extern "C" int vsr_convolve(const void* src, int dtype, int64_t height, int64_t 
   if (precision < VSR_PREC_AUTO || precision > VSR_PREC_SPLIT_BF16) return fail(VSR_ERR_INVALID_ARG, "bad precision %d", precision);
   if (kh > kMaxDirectK || kw > kMaxDirectK)
     return fail(VSR_ERR_UNSUPPORTED, "kernel %dx%d larger than the supported %dx%d", kh, kw, kMaxDirectK, kMaxDirectK);
-  if (precision == VSR_PREC_SPLIT_BF16) return fail(VSR_ERR_UNSUPPORTED, "split-BF16 convolution not in this build");
+  // Tensor-core path: float32 rasters with 16-byte aligned rows, kernels that
+  // fit its shared-memory plan; AUTO takes it for k >= 15 on both axes.
+  const bool tc_ok = dtype == VSR_F32 && conv_tc_supported(kh, kw) && aligned(src, 16) && pitch % 4 == 0;
+  if (precision == VSR_PREC_SPLIT_BF16 && !tc_ok)
+    return fail(VSR_ERR_UNSUPPORTED,
+                "split-BF16 convolution needs a float32 raster with 16-byte aligned rows and a kernel of at most 41x41");
+  if (precision == VSR_PREC_SPLIT_BF16 || (precision == VSR_PREC_AUTO && tc_ok && kh >= 15 && kw >= 15))
+    return run_conv_tc(src, dtype, height, width, pitch, weights_host, kh, kw, nodata, nodata_kind, dst, out_dtype,
+                       out_pitch, workspace, workspace_bytes, static_cast<cudaStream_t>(stream));
   const size_t need = conv_ws_plain(kh, kw);
   if (!workspace || workspace_bytes < need || !aligned(workspace, 256))
     return fail(VSR_ERR_WORKSPACE, "workspace must be 256-byte aligned and >= %zu bytes", need);

@@ -7,10 +7,11 @@
 // boundary (ctypes / cgo / JNI) without access to the process allocator, or
 // code that issues work while a CUDA graph is captured in a mode that
 // forbids allocation.  For them this entry point takes only the inputs and
-// the output; its scratch (the staged float64 weights, the float32 weight
-// rows and the weight total) lives in a file-scope __device__ array sized
-// for the largest supported kernel.  Every GPU that loads the library holds
-// that array (kNoAllocScratchBytes) until the process exits.
+// the output; its scratch (the staged float64 weights and the float32 or
+// BF16 operand images built from them) lives in a file-scope __device__ array sized
+// for the largest supported kernel of either precision.  Every GPU that
+// loads the library holds that array (kNoAllocScratchBytes, 105.75 KiB)
+// until the process exits.
 //
 // Host code cannot use the array's name as a device address, so on the first
 // call on each device (with that device current) the address is resolved
@@ -30,9 +31,12 @@ size_t conv_ws_plain(int kh, int kw);  // focal.cu
 namespace {
 
 constexpr int kNoAllocMaxK = 80;
-// conv_ws_plain(80, 80): 51,200 B float64 weights + 25,600 B float32 rows +
-// 256 B for the total = 77,056 B.
-constexpr size_t kNoAllocScratchBytes = 77056;
+// The larger of the two workspaces vsr_convolve can ask for:
+//  * FP32 path, 80 x 80: 51,200 B float64 weights + 25,600 B float32 rows +
+//    256 B for the total = 77,056 B;
+//  * split-BF16 path, 41 x 41: 13,568 B float64 weights + 94,464 B Toeplitz
+//    images + 256 B = 108,288 B.
+constexpr size_t kNoAllocScratchBytes = 108288;
 
 static __device__ __align__(256) unsigned char g_conv_scratch[kNoAllocScratchBytes];
 

@@ -29,6 +29,8 @@
 //    hillshade stores.
 //  * horn_generic  -- every other dtype / alignment: one thread per pixel,
 //    clamped loads through L1.
+#include <vector>
+
 #include "vsr_internal.cuh"
 
 namespace vsr {
@@ -143,6 +145,20 @@ __device__ __forceinline__ PixelOut horn_pixel(float gx, float gy, const HornPar
   return o;
 }
 
+constexpr int kWantSlope = 1, kWantAspect = 2, kWantHs = 4;
+
+// The wanted outputs are a compile-time set, so the per-pixel path has no
+// branches on which outputs exist.
+template <int WANT>
+__device__ __forceinline__ void horn_px(float gx, float gy, const HornParams& P, float& so, float& ao, uint8_t& ho) {
+  const float p = gx * P.inv8cx;
+  const float q = gy * P.inv8cy;
+  const float s = fmaf(p, p, q * q);
+  if (WANT & kWantSlope) so = slope_deg(s);
+  if (WANT & kWantAspect) ao = aspect_deg(p, q);
+  if (WANT & kWantHs) ho = hillshade_u8(p, q, s, P);
+}
+
 // ------------------------------------------------------------ TMA kernel --
 constexpr int kTW = 128;        // output tile width (32 lanes x 4 pixels)
 constexpr int kSW = kTW + 8;    // staged width: 4-column halo each side (16 B)
@@ -175,106 +191,117 @@ __device__ __forceinline__ uint32_t nd_bits6(const float v[6], int kind, float n
   return m;
 }
 
+// Load one staged row for a lane: 6 values, its 4 horizontal differences
+// (x+2 minus x, shared by the three output rows that use the row) and, for
+// masked tiles, its 6 nodata bits.
+template <bool MASKED>
+__device__ __forceinline__ void stage_row(const float* row, int lane, const HornParams& P, float nd_in, float v[6],
+                                          float hd[4], uint32_t& m) {
+  load6(row, lane, v);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) hd[k] = v[k + 2] - v[k];
+  m = MASKED ? nd_bits6(v, P.nd_kind, nd_in) : 0u;
+}
+
+// One output row (4 pixels of this lane) from the rows above (t) and below
+// (b), the three rows' horizontal differences and nodata bits.
+template <int WANT, bool MASKED, bool EDGE, bool VEC = true>
+__device__ __forceinline__ void horn_out_row(const float t[6], const float b[6], const float hdt[4],
+                                             const float hdm[4], const float hdb[4], uint32_t mt, uint32_t mm,
+                                             uint32_t mb, const HornParams& P, const MaskRule& rule, int64_t y,
+                                             int64_t xs, float* __restrict__ srow, float* __restrict__ arow,
+                                             uint8_t* __restrict__ hrow) {
+  if (EDGE && (y >= P.height || xs >= P.width)) return;
+  float dv[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) dv[k] = b[k] - t[k];
+  float so[4], ao[4];
+  uint8_t ho[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float gx = fmaf(2.0f, hdm[k], hdt[k] + hdb[k]);
+    const float gy = fmaf(2.0f, dv[k + 1], dv[k] + dv[k + 2]);
+    horn_px<WANT>(gx, gy, P, so[k], ao[k], ho[k]);
+  }
+  if (MASKED) {
+    const uint32_t hdil = (mt | (mt >> 1) | (mt >> 2)) | (mm | (mm >> 1) | (mm >> 2)) | (mb | (mb >> 1) | (mb >> 2));
+    const uint32_t sabits = rule.sa_any ? (rule.sa_center ? (mm >> 1) : hdil) : 0u;
+    const uint32_t hsbits = rule.hs_any ? hdil : 0u;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const bool sa_nd = (sabits >> k) & 1u;
+      so[k] = sa_nd ? P.nd_out_f : so[k];
+      ao[k] = sa_nd ? P.nd_out_f : ao[k];
+      ho[k] = ((hsbits >> k) & 1u) ? uint8_t(0) : ho[k];
+    }
+  }
+  const bool full = VEC && (!EDGE || xs + 3 < P.width);
+  if (full) {
+    if (WANT & kWantSlope) __stcs(reinterpret_cast<float4*>(srow), make_float4(so[0], so[1], so[2], so[3]));
+    if (WANT & kWantAspect) __stcs(reinterpret_cast<float4*>(arow), make_float4(ao[0], ao[1], ao[2], ao[3]));
+    if (WANT & kWantHs)
+      __stcs(reinterpret_cast<unsigned int*>(hrow), uint32_t(ho[0]) | (uint32_t(ho[1]) << 8) |
+                                                         (uint32_t(ho[2]) << 16) | (uint32_t(ho[3]) << 24));
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (xs + k < P.width) {
+        if (WANT & kWantSlope) srow[k] = so[k];
+        if (WANT & kWantAspect) arow[k] = ao[k];
+        if (WANT & kWantHs) hrow[k] = ho[k];
+      }
+    }
+  }
+}
+
 // RB output rows of one warp: rows r0 .. r0+RB-1 of the tile (staged rows
-// r0 .. r0+RB+1), lane columns xs .. xs+3.  Horizontal differences of a staged
-// row are formed once and reused by the three output rows that need them.
-template <int RB, bool MASKED>
+// r0 .. r0+RB+1), lane columns xs .. xs+3.  Two output rows per iteration
+// (rolled on purpose: a fully unrolled loop overflowed the instruction cache).
+template <int RB, int WANT, bool MASKED, bool EDGE, bool VEC = true>
 __device__ __forceinline__ void horn_rows(const float* S, int lane, int r0, int64_t y0, int64_t xs,
                                           const HornParams& P, const MaskRule& rule, float nd_in,
                                           float* __restrict__ slope, float* __restrict__ aspect,
                                           uint8_t* __restrict__ hs) {
-  const int64_t W = P.width, H = P.height;
-  const bool want_s = slope != nullptr, want_a = aspect != nullptr, want_h = hs != nullptr;
-  float top[6], mid[6], bot[6];
-  float hdt[4], hdm[4], hdb[4];
-  load6(S + (r0 + 0) * kSW, lane, top);
-  load6(S + (r0 + 1) * kSW, lane, mid);
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    hdt[k] = top[k + 2] - top[k];
-    hdm[k] = mid[k + 2] - mid[k];
-  }
-  uint32_t mt = 0, mm = 0;
-  if (MASKED) {
-    mt = nd_bits6(top, P.nd_kind, nd_in);
-    mm = nd_bits6(mid, P.nd_kind, nd_in);
-  }
-  // Rolled on purpose: a fully unrolled row loop overflows the instruction
-  // cache (ncu: "no instruction" stalls dominated).
+  static_assert(RB % 2 == 0, "two output rows per iteration");
+  float v0[6], v1[6], hd0[4], hd1[4];
+  uint32_t m0, m1;
+  stage_row<MASKED>(S + (r0 + 0) * kSW, lane, P, nd_in, v0, hd0, m0);
+  stage_row<MASKED>(S + (r0 + 1) * kSW, lane, P, nd_in, v1, hd1, m1);
+  const int64_t y = y0 + r0;
+  float* srow = (WANT & kWantSlope) ? slope + y * P.out_pitch + xs : nullptr;
+  float* arow = (WANT & kWantAspect) ? aspect + y * P.out_pitch + xs : nullptr;
+  uint8_t* hrow = (WANT & kWantHs) ? hs + y * P.hs_pitch + xs : nullptr;
 #pragma unroll 1
-  for (int j = 0; j < RB; ++j) {
-    load6(S + (r0 + j + 2) * kSW, lane, bot);
-    float dv[6];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) dv[k] = bot[k] - top[k];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) hdb[k] = bot[k + 2] - bot[k];
-    uint32_t mb = 0;
-    if (MASKED) mb = nd_bits6(bot, P.nd_kind, nd_in);
-    const int64_t y = y0 + r0 + j;
-    if (y < H && xs < W) {
-      uint32_t hdil = 0, ctr = 0;
-      if (MASKED) {
-        hdil = (mt | (mt >> 1) | (mt >> 2)) | (mm | (mm >> 1) | (mm >> 2)) | (mb | (mb >> 1) | (mb >> 2));
-        ctr = mm >> 1;
-      }
-      float so[4], ao[4];
-      uint8_t ho[4];
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const float gx = fmaf(2.0f, hdm[k], hdt[k] + hdb[k]);
-        const float gy = fmaf(2.0f, dv[k + 1], dv[k] + dv[k + 2]);
-        const PixelOut o = horn_pixel(gx, gy, P, want_s, want_a, want_h);
-        so[k] = o.slope;
-        ao[k] = o.aspect;
-        ho[k] = o.hs;
-        if (MASKED) {
-          const bool sa_nd = rule.sa_any && (((rule.sa_center ? ctr : hdil) >> k) & 1u);
-          const bool hs_nd = rule.hs_any && ((hdil >> k) & 1u);
-          so[k] = sa_nd ? P.nd_out_f : so[k];
-          ao[k] = sa_nd ? P.nd_out_f : ao[k];
-          ho[k] = hs_nd ? uint8_t(0) : ho[k];
-        }
-      }
-      const bool full = xs + 3 < W;
-      if (want_s) {
-        float* dst = slope + y * P.out_pitch + xs;
-        if (full) __stcs(reinterpret_cast<float4*>(dst), make_float4(so[0], so[1], so[2], so[3]));
-        else for (int k = 0; k < 4; ++k) if (xs + k < W) __stcs(dst + k, so[k]);
-      }
-      if (want_a) {
-        float* dst = aspect + y * P.out_pitch + xs;
-        if (full) __stcs(reinterpret_cast<float4*>(dst), make_float4(ao[0], ao[1], ao[2], ao[3]));
-        else for (int k = 0; k < 4; ++k) if (xs + k < W) __stcs(dst + k, ao[k]);
-      }
-      if (want_h) {
-        uint8_t* dst = hs + y * P.hs_pitch + xs;
-        if (full) {
-          const uint32_t packed = uint32_t(ho[0]) | (uint32_t(ho[1]) << 8) | (uint32_t(ho[2]) << 16) |
-                                  (uint32_t(ho[3]) << 24);
-          __stcs(reinterpret_cast<unsigned int*>(dst), packed);
-        } else {
-          for (int k = 0; k < 4; ++k) if (xs + k < W) dst[k] = ho[k];
-        }
-      }
-    }
+  for (int j = 0; j < RB; j += 2) {
+    float v2[6], v3[6], hd2[4], hd3[4];
+    uint32_t m2, m3;
+    stage_row<MASKED>(S + (r0 + j + 2) * kSW, lane, P, nd_in, v2, hd2, m2);
+    stage_row<MASKED>(S + (r0 + j + 3) * kSW, lane, P, nd_in, v3, hd3, m3);
+    horn_out_row<WANT, MASKED, EDGE, VEC>(v0, v2, hd0, hd1, hd2, m0, m1, m2, P, rule, y + j, xs, srow, arow, hrow);
+    if (WANT & kWantSlope) srow += P.out_pitch;
+    if (WANT & kWantAspect) arow += P.out_pitch;
+    if (WANT & kWantHs) hrow += P.hs_pitch;
+    horn_out_row<WANT, MASKED, EDGE, VEC>(v1, v3, hd1, hd2, hd3, m1, m2, m3, P, rule, y + j + 1, xs, srow, arow, hrow);
+    if (WANT & kWantSlope) srow += P.out_pitch;
+    if (WANT & kWantAspect) arow += P.out_pitch;
+    if (WANT & kWantHs) hrow += P.hs_pitch;
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
-      top[k] = mid[k];
-      mid[k] = bot[k];
+      v0[k] = v2[k];
+      v1[k] = v3[k];
     }
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      hdt[k] = hdm[k];
-      hdm[k] = hdb[k];
+      hd0[k] = hd2[k];
+      hd1[k] = hd3[k];
     }
-    mt = mm;
-    mm = mb;
+    m0 = m2;
+    m1 = m3;
   }
 }
 
-template <int TH, int STAGES, int THREADS>
-__global__ void __launch_bounds__(THREADS) horn_f32_tma(const __grid_constant__ CUtensorMap tmap,
+template <int TH, int STAGES, int THREADS, int WANT>
+__global__ void __launch_bounds__(THREADS, 768 / THREADS) horn_f32_tma(const __grid_constant__ CUtensorMap tmap,
                                                         const HornParams P, const float nd_in,
                                                         float* __restrict__ slope,
                                                         float* __restrict__ aspect,
@@ -369,10 +396,14 @@ __global__ void __launch_bounds__(THREADS) horn_f32_tma(const __grid_constant__ 
     const bool masked = __syncthreads_or(any_nd);
 
     const int64_t xs = x0 + 4 * lane;
-    if (masked)
-      horn_rows<RB, true>(S, lane, warp * RB, y0, xs, P, rule, nd_in, slope, aspect, hs);
-    else
-      horn_rows<RB, false>(S, lane, warp * RB, y0, xs, P, rule, nd_in, slope, aspect, hs);
+    const bool edge = x0 + kTW > W || y0 + TH > H;
+    if (masked) {
+      if (edge) horn_rows<RB, WANT, true, true>(S, lane, warp * RB, y0, xs, P, rule, nd_in, slope, aspect, hs);
+      else horn_rows<RB, WANT, true, false>(S, lane, warp * RB, y0, xs, P, rule, nd_in, slope, aspect, hs);
+    } else {
+      if (edge) horn_rows<RB, WANT, false, true>(S, lane, warp * RB, y0, xs, P, rule, nd_in, slope, aspect, hs);
+      else horn_rows<RB, WANT, false, false>(S, lane, warp * RB, y0, xs, P, rule, nd_in, slope, aspect, hs);
+    }
 
     __syncthreads();  // every read of stage s is done
     if (tid == 0) {
@@ -455,7 +486,7 @@ int dispatch_generic(int dtype, const void* src, const HornParams& P, double ndv
   }
 }
 
-template <int TH, int STAGES, int THREADS>
+template <int TH, int STAGES, int THREADS, int WANT>
 int launch_tma(const void* src, const HornParams& P, float nd_in, float* slope, float* aspect,
                uint8_t* hs, cudaStream_t st) {
   using Tile = TmaTile<TH>;
@@ -466,7 +497,7 @@ int launch_tma(const void* src, const HornParams& P, float nd_in, float* slope, 
   uint32_t* err = device_error_word();
   if (!err) return VSR_ERR_CUDA;
   const size_t smem = STAGES * Tile::kStride + 1024;
-  auto kern = horn_f32_tma<TH, STAGES, THREADS>;
+  auto kern = horn_f32_tma<TH, STAGES, THREADS, WANT>;
   VSR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   int per_sm = 0;
   VSR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, THREADS, smem));
@@ -483,17 +514,30 @@ int launch_tma(const void* src, const HornParams& P, float nd_in, float* slope, 
 struct HornConfig {
   int th, stages, threads;
 };
-constexpr HornConfig kHornConfigs[] = {{32, 3, 256}, {64, 2, 256}, {16, 4, 128}, {32, 2, 128}, {64, 3, 256}};
+constexpr HornConfig kHornConfigs[] = {{64, 2, 256}, {32, 2, 128}, {32, 3, 256}};
 constexpr int kNumHornConfigs = sizeof(kHornConfigs) / sizeof(kHornConfigs[0]);
+
+template <int WANT>
+int launch_tma_want(int cfg, const void* src, const HornParams& P, float nd_in, float* slope, float* aspect,
+                    uint8_t* hs, cudaStream_t st) {
+  switch (cfg) {
+    case 1: return launch_tma<32, 2, 128, WANT>(src, P, nd_in, slope, aspect, hs, st);
+    case 2: return launch_tma<32, 3, 256, WANT>(src, P, nd_in, slope, aspect, hs, st);
+    default: return launch_tma<64, 2, 256, WANT>(src, P, nd_in, slope, aspect, hs, st);
+  }
+}
 
 int launch_tma_config(int cfg, const void* src, const HornParams& P, float nd_in, float* slope,
                       float* aspect, uint8_t* hs, cudaStream_t st) {
-  switch (cfg) {
-    case 1: return launch_tma<64, 2, 256>(src, P, nd_in, slope, aspect, hs, st);
-    case 2: return launch_tma<16, 4, 128>(src, P, nd_in, slope, aspect, hs, st);
-    case 3: return launch_tma<32, 2, 128>(src, P, nd_in, slope, aspect, hs, st);
-    case 4: return launch_tma<64, 3, 256>(src, P, nd_in, slope, aspect, hs, st);
-    default: return launch_tma<32, 3, 256>(src, P, nd_in, slope, aspect, hs, st);
+  const int want = (slope ? kWantSlope : 0) | (aspect ? kWantAspect : 0) | (hs ? kWantHs : 0);
+  switch (want) {
+    case 1: return launch_tma_want<1>(cfg, src, P, nd_in, slope, aspect, hs, st);
+    case 2: return launch_tma_want<2>(cfg, src, P, nd_in, slope, aspect, hs, st);
+    case 3: return launch_tma_want<3>(cfg, src, P, nd_in, slope, aspect, hs, st);
+    case 4: return launch_tma_want<4>(cfg, src, P, nd_in, slope, aspect, hs, st);
+    case 5: return launch_tma_want<5>(cfg, src, P, nd_in, slope, aspect, hs, st);
+    case 6: return launch_tma_want<6>(cfg, src, P, nd_in, slope, aspect, hs, st);
+    default: return launch_tma_want<7>(cfg, src, P, nd_in, slope, aspect, hs, st);
   }
 }
 
@@ -560,4 +604,353 @@ extern "C" int vsr_horn_fused(const void* dem, int dtype, int64_t height, int64_
   if ((slope || aspect) && out_dtype == VSR_F64)
     return dispatch_generic<double>(dtype, dem, P, ndv, slope, aspect, hillshade, st);
   return dispatch_generic<float>(dtype, dem, P, ndv, slope, aspect, hillshade, st);
+}
+
+// ===================================================================== batch ==
+// One persistent, work-queue-scheduled launch over many DEM tiles of uneven
+// sizes, each with its own cell size and nodata: slope + aspect (Horn) and a
+// KG x KG nodata-aware Gaussian, all from one staged block.  Replaces the
+// reference's per-tile / per-band Python loops (dispatch.py:417-506), which
+// issue separate launches per raster and per operation.
+//
+// Work item = (tile, 128 x TH output block).  A CTA claims items with an
+// atomic counter (no waits: an exhausted queue simply ends the CTA), finds
+// the tile by binary search over the per-tile prefix sums, stages
+// (TH + 2*HY) x 136 input values with coalesced loads and clamped
+// coordinates (any pitch or alignment; edge replication for Horn), runs the
+// Horn rows on them, then the separable Gaussian: a row pass into shared
+// memory (numerator and weight sum, validity from coordinates and nodata so
+// out-of-bounds taps are skipped), then the column pass.
+namespace vsr {
+namespace {
+
+struct BatchTileDev {
+  const float* src;
+  int64_t H, W, pitch;
+  float* slope;
+  float* aspect;
+  float* smooth;
+  int64_t out_pitch;
+  double cell_x, cell_y, nodata;
+  int32_t nd_kind;
+  uint32_t flags;
+  int64_t first_item;  // prefix sum of items over earlier tiles
+  int64_t items_x;     // blocks across this tile
+  int32_t vec;         // outputs 16-byte aligned with pitch % 4 == 0
+  int32_t pad_;
+};
+
+struct BatchHeader {  // at the start of the plan
+  unsigned long long counter;
+  int64_t total_items;
+  int32_t n_tiles, kg, th, threads;
+  float g[16];          // Gaussian taps (float32 of the float64 weights)
+  float gsum;           // sum of g
+  float pad_[3];
+};
+
+constexpr int kBatchMaxKG = 9;
+
+template <int TH, int THREADS, int KG>
+struct BatchSmem {
+  static constexpr int HY = KG / 2 > 0 ? KG / 2 : 1;  // staged halo rows (>= 1 for Horn)
+  static constexpr int SR = TH + 2 * HY;              // staged rows
+  static constexpr int kFloats = SR * kSW + 2 * SR * kTW;
+};
+
+template <int TH, int THREADS, int KG>
+__global__ void __launch_bounds__(THREADS) batch_terrain_kernel(BatchHeader* __restrict__ hdr,
+                                                                const BatchTileDev* __restrict__ tiles) {
+  using L = BatchSmem<TH, THREADS, KG>;
+  constexpr int WARPS = THREADS / 32;
+  constexpr int RB = TH / WARPS;
+  constexpr int HY = L::HY, SR = L::SR;
+  static_assert(RB * WARPS == TH && RB % 2 == 0, "rows per warp");
+  extern __shared__ __align__(16) float bsm[];
+  float* S = bsm;                 // SR x kSW staged values
+  float* Rn = S + SR * kSW;       // SR x kTW row-pass numerator
+  float* Rd = Rn + SR * kTW;      // SR x kTW row-pass weight sum
+  __shared__ int64_t sh_item;
+  __shared__ int sh_tile;
+  __shared__ HornParams sh_P;
+  __shared__ float sh_nd;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t total = hdr->total_items;
+  const int n_tiles = hdr->n_tiles;
+
+  for (;;) {
+    if (tid == 0) {
+      const int64_t item = static_cast<int64_t>(atomicAdd(&hdr->counter, 1ull));
+      sh_item = item;
+      if (item < total) {
+        int lo = 0, hi = n_tiles - 1;  // last tile with first_item <= item
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (tiles[mid].first_item <= item) lo = mid;
+          else hi = mid - 1;
+        }
+        sh_tile = lo;
+        const BatchTileDev& T = tiles[lo];
+        HornParams P{};
+        P.height = T.H;
+        P.width = T.W;
+        P.in_pitch = T.pitch;
+        P.out_pitch = T.out_pitch;
+        P.hs_pitch = T.out_pitch;
+        // per-tile cell-size scale formed in FP64 on the device
+        P.inv8cx = static_cast<float>(1.0 / (8.0 * T.cell_x));
+        P.inv8cy = static_cast<float>(1.0 / (8.0 * T.cell_y));
+        P.nd_out_f = static_cast<float>(T.nodata);
+        P.nd_out_d = T.nodata;
+        P.flags = T.flags;
+        P.nd_kind = T.nd_kind;
+        sh_P = P;
+        sh_nd = static_cast<float>(T.nodata);
+      }
+    }
+    __syncthreads();
+    const int64_t item = sh_item;
+    if (item >= total) break;
+    const BatchTileDev& T = tiles[sh_tile];
+    const HornParams P = sh_P;
+    const float nd_in = sh_nd;
+    const int64_t local = item - T.first_item;
+    const int64_t by = local / T.items_x, bx = local - by * T.items_x;
+    const int64_t x0 = bx * kTW, y0 = by * TH;
+    const int64_t H = T.H, W = T.W;
+
+    // Stage rows y0-HY .. y0+TH+HY-1, columns x0-4 .. x0+131 (clamped).
+    bool any_nd = false;
+    for (int i = tid; i < SR * kSW; i += THREADS) {
+      const int r = i / kSW, c = i - r * kSW;
+      const int64_t gy = min(max(y0 - HY + r, int64_t(0)), H - 1);
+      const int64_t gx = min(max(x0 - 4 + c, int64_t(0)), W - 1);
+      const float v = __ldg(T.src + gy * T.pitch + gx);
+      S[i] = v;
+      any_nd |= is_nd(v, P.nd_kind, nd_in);
+    }
+    const bool masked = __syncthreads_or(any_nd);
+    const bool edge = x0 + kTW > W || y0 + TH > H;
+    const MaskRule rule = mask_rule(P);
+
+    // Horn slope + aspect.
+    if (T.slope || T.aspect) {
+      const int64_t xs = x0 + 4 * lane;
+      const float* Sh = S + (HY - 1) * kSW;
+      // both outputs are requested together in the batch plan
+      if (T.vec) {
+        if (masked) {
+          if (edge) horn_rows<RB, 3, true, true, true>(Sh, lane, warp * RB, y0, xs, P, rule, nd_in, T.slope, T.aspect, nullptr);
+          else horn_rows<RB, 3, true, false, true>(Sh, lane, warp * RB, y0, xs, P, rule, nd_in, T.slope, T.aspect, nullptr);
+        } else {
+          if (edge) horn_rows<RB, 3, false, true, true>(Sh, lane, warp * RB, y0, xs, P, rule, nd_in, T.slope, T.aspect, nullptr);
+          else horn_rows<RB, 3, false, false, true>(Sh, lane, warp * RB, y0, xs, P, rule, nd_in, T.slope, T.aspect, nullptr);
+        }
+      } else {
+        if (masked) horn_rows<RB, 3, true, true, false>(Sh, lane, warp * RB, y0, xs, P, rule, nd_in, T.slope, T.aspect, nullptr);
+        else horn_rows<RB, 3, false, true, false>(Sh, lane, warp * RB, y0, xs, P, rule, nd_in, T.slope, T.aspect, nullptr);
+      }
+    }
+
+    // Gaussian KG x KG (normalised, nodata-aware, out-of-bounds taps skipped).
+    if (T.smooth) {
+      constexpr int R = KG / 2;
+      const bool exact_den = masked || x0 - R < 0 || y0 - R < 0 || x0 + kTW + R > W || y0 + TH + R > H;
+      // row pass: staged rows (HY-R) .. (HY+TH+R-1), 4 columns per lane
+      for (int r = warp + (HY - R); r < HY + TH + R; r += WARPS) {
+        const int64_t gy = y0 - HY + r;
+        const bool row_in = gy >= 0 && gy < H;
+        const int c0 = 4 * lane;
+        float z[4 + KG - 1], vd[4 + KG - 1];
+#pragma unroll
+        for (int j = 0; j < 4 + KG - 1; ++j) {
+          const int c = c0 + 4 - R + j;  // staged column
+          const float v = S[r * kSW + c];
+          const int64_t gx = x0 - 4 + c;
+          const bool ok = row_in && gx >= 0 && gx < W && !is_nd(v, P.nd_kind, nd_in);
+          z[j] = v * (ok ? 1.0f : 0.0f);  // NaN * 0 stays NaN, as in the reference
+          vd[j] = ok ? 1.0f : 0.0f;
+        }
+        float an[4] = {}, ad[4] = {};
+#pragma unroll
+        for (int t = 0; t < KG; ++t) {
+          const float w = hdr->g[t];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            an[u] = fmaf(w, z[u + t], an[u]);
+            ad[u] = fmaf(w, vd[u + t], ad[u]);
+          }
+        }
+        *reinterpret_cast<float4*>(Rn + r * kTW + c0) = make_float4(an[0], an[1], an[2], an[3]);
+        *reinterpret_cast<float4*>(Rd + r * kTW + c0) = make_float4(ad[0], ad[1], ad[2], ad[3]);
+      }
+      __syncthreads();
+      // column pass: one column per thread, TH*kTW/THREADS consecutive rows
+      constexpr int GROUPS = THREADS / kTW;
+      constexpr int RY = TH / GROUPS;
+      const int c = tid % kTW;
+      const int q0 = (tid / kTW) * RY;
+      const int64_t x = x0 + c;
+      const float gs2 = hdr->gsum * hdr->gsum;
+#pragma unroll 1
+      for (int q = q0; q < q0 + RY; ++q) {
+        const int64_t y = y0 + q;
+        if (y >= H || x >= W) continue;
+        float num = 0.0f, den = 0.0f;
+#pragma unroll
+        for (int t = 0; t < KG; ++t) {
+          const int r = q + HY - R + t;
+          const float w = hdr->g[t];
+          num = fmaf(w, Rn[r * kTW + c], num);
+          den = fmaf(w, Rd[r * kTW + c], den);
+        }
+        if (!exact_den) den = gs2;
+        const float cv = S[(q + HY) * kSW + c + 4];
+        const bool centre_ok = !is_nd(cv, P.nd_kind, nd_in);
+        T.smooth[y * T.out_pitch + x] = (centre_ok && den > 0.0f) ? num / den : P.nd_out_f;
+      }
+    }
+    __syncthreads();  // staged block and row pass are reused by the next item
+  }
+}
+
+// Launch configurations the autotuner chooses between: (rows per block,
+// threads per CTA); the Gaussian width is a template parameter too.
+struct BatchConfig {
+  int th, threads;
+};
+constexpr BatchConfig kBatchConfigs[] = {{32, 256}, {64, 256}, {16, 128}, {32, 128}};
+constexpr int kNumBatchConfigs = sizeof(kBatchConfigs) / sizeof(kBatchConfigs[0]);
+
+template <int TH, int THREADS, int KG>
+int launch_batch_t(BatchHeader* hdr, const BatchTileDev* tiles, cudaStream_t st) {
+  using L = BatchSmem<TH, THREADS, KG>;
+  const size_t smem = static_cast<size_t>(L::kFloats) * 4;
+  auto kern = batch_terrain_kernel<TH, THREADS, KG>;
+  VSR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  int per_sm = 0;
+  VSR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, THREADS, smem));
+  if (per_sm < 1) return fail(VSR_ERR_CUDA, "batch kernel cannot be resident");
+  kern<<<static_cast<unsigned>(sm_count() * per_sm), THREADS, smem, st>>>(hdr, tiles);
+  VSR_CUDA_TRY(cudaGetLastError());
+  return VSR_OK;
+}
+
+template <int KG>
+int launch_batch_kg(int cfg, BatchHeader* hdr, const BatchTileDev* tiles, cudaStream_t st) {
+  switch (cfg) {
+    case 1: return launch_batch_t<64, 256, KG>(hdr, tiles, st);
+    case 2: return launch_batch_t<16, 128, KG>(hdr, tiles, st);
+    case 3: return launch_batch_t<32, 128, KG>(hdr, tiles, st);
+    default: return launch_batch_t<32, 256, KG>(hdr, tiles, st);
+  }
+}
+
+__global__ void prep_batch_gauss(BatchHeader* hdr, int kg, double sigma) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double s = 0.0;
+  for (int i = 0; i < kg; ++i) {
+    const double a = (i - kg / 2) / sigma;
+    const double g = exp(-0.5 * a * a);
+    hdr->g[i] = static_cast<float>(g);
+    s += static_cast<double>(static_cast<float>(g));
+  }
+  hdr->gsum = static_cast<float>(s);
+}
+
+}  // namespace
+
+int batch_config_count() { return kNumBatchConfigs; }
+
+}  // namespace vsr
+
+extern "C" size_t vsr_batch_plan_size(int n_tiles) {
+  if (n_tiles <= 0) return 0;
+  return ((sizeof(vsr::BatchHeader) + 255) & ~size_t(255)) + static_cast<size_t>(n_tiles) * sizeof(vsr::BatchTileDev);
+}
+
+extern "C" int vsr_batch_plan(const vsr_batch_tile* tiles_host, int n_tiles, double sigma, int gauss_k, void* plan,
+                              size_t plan_bytes, int64_t* total_items, void* stream) {
+  using namespace vsr;
+  if (n_tiles <= 0 || !tiles_host) return fail(VSR_ERR_INVALID_ARG, "need at least one tile");
+  if (gauss_k != 0 && (gauss_k < 1 || gauss_k > kBatchMaxKG || gauss_k % 2 == 0))
+    return fail(VSR_ERR_UNSUPPORTED, "batch Gaussian size must be odd and <= %d", kBatchMaxKG);
+  if (gauss_k != 0 && !(sigma > 0.0)) return fail(VSR_ERR_INVALID_ARG, "sigma must be positive, got %g", sigma);
+  const size_t need = vsr_batch_plan_size(n_tiles);
+  if (!plan || plan_bytes < need || !aligned(plan, 256))
+    return fail(VSR_ERR_WORKSPACE, "plan must be 256-byte aligned and >= %zu bytes", need);
+  const int cfg = tuning_get(VSR_OP_BATCH);
+  const int th = kBatchConfigs[cfg].th;
+  std::vector<BatchTileDev> dev(n_tiles);
+  int64_t items = 0;
+  for (int i = 0; i < n_tiles; ++i) {
+    const vsr_batch_tile& t = tiles_host[i];
+    if (t.height <= 0 || t.width <= 0 || !t.src) return fail(VSR_ERR_INVALID_ARG, "tile %d is empty or NULL", i);
+    if (t.pitch < t.width || t.out_pitch < t.width) return fail(VSR_ERR_INVALID_ARG, "tile %d: pitch < width", i);
+    if (!(t.cell_x > 0.0) || !(t.cell_y > 0.0)) return fail(VSR_ERR_INVALID_ARG, "tile %d: cell sizes must be positive", i);
+    if ((t.slope == nullptr) != (t.aspect == nullptr))
+      return fail(VSR_ERR_INVALID_ARG, "tile %d: slope and aspect are produced together", i);
+    if (!aligned(t.src, 4) || (t.slope && !aligned(t.slope, 4)) || (t.aspect && !aligned(t.aspect, 4)) ||
+        (t.smooth && !aligned(t.smooth, 4)))
+      return fail(VSR_ERR_INVALID_ARG, "tile %d: buffers must be 4-byte aligned", i);
+    if (t.smooth && gauss_k == 0) return fail(VSR_ERR_INVALID_ARG, "tile %d wants a Gaussian but gauss_k is 0", i);
+    BatchTileDev& d = dev[i];
+    d.src = t.src;
+    d.H = t.height;
+    d.W = t.width;
+    d.pitch = t.pitch;
+    d.slope = t.slope;
+    d.aspect = t.aspect;
+    d.smooth = t.smooth;
+    d.out_pitch = t.out_pitch;
+    d.cell_x = t.cell_x;
+    d.cell_y = t.cell_y;
+    d.nodata = t.nodata;
+    double ev = 0.0;
+    d.nd_kind = resolve_nodata(VSR_F32, t.nodata, t.nodata_kind, &ev);
+    d.flags = t.flags;
+    d.vec = (!t.slope || (aligned(t.slope, 16) && aligned(t.aspect, 16))) && t.out_pitch % 4 == 0;
+    d.pad_ = 0;
+    d.items_x = (t.width + kTW - 1) / kTW;
+    d.first_item = items;
+    items += d.items_x * ((t.height + th - 1) / th);
+  }
+  BatchHeader h{};
+  h.counter = 0;
+  h.total_items = items;
+  h.n_tiles = n_tiles;
+  h.kg = gauss_k;
+  h.th = th;
+  h.threads = kBatchConfigs[cfg].threads;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  char* base = static_cast<char*>(plan);
+  const size_t off = (sizeof(BatchHeader) + 255) & ~size_t(255);
+  VSR_CUDA_TRY(cudaMemcpyAsync(base, &h, sizeof(h), cudaMemcpyHostToDevice, st));
+  VSR_CUDA_TRY(cudaMemcpyAsync(base + off, dev.data(), dev.size() * sizeof(BatchTileDev), cudaMemcpyHostToDevice, st));
+  if (gauss_k) {
+    prep_batch_gauss<<<1, 32, 0, st>>>(reinterpret_cast<BatchHeader*>(base), gauss_k, sigma);
+    VSR_CUDA_TRY(cudaGetLastError());
+  }
+  VSR_CUDA_TRY(cudaStreamSynchronize(st));  // the host descriptors are staged from pageable memory
+  if (total_items) *total_items = items;
+  return VSR_OK;
+}
+
+extern "C" int vsr_batch_run(void* plan, int gauss_k, void* stream) {
+  using namespace vsr;
+  if (!plan || !aligned(plan, 256)) return fail(VSR_ERR_INVALID_ARG, "plan must be a 256-byte aligned device pointer");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  BatchHeader* hdr = static_cast<BatchHeader*>(plan);
+  const BatchTileDev* tiles = reinterpret_cast<const BatchTileDev*>(static_cast<char*>(plan) + ((sizeof(BatchHeader) + 255) & ~size_t(255)));
+  VSR_CUDA_TRY(cudaMemsetAsync(&hdr->counter, 0, sizeof(hdr->counter), st));
+  const int cfg = tuning_get(VSR_OP_BATCH);
+  switch (gauss_k) {
+    case 0:
+    case 1: return launch_batch_kg<1>(cfg, hdr, tiles, st);
+    case 3: return launch_batch_kg<3>(cfg, hdr, tiles, st);
+    case 5: return launch_batch_kg<5>(cfg, hdr, tiles, st);
+    case 7: return launch_batch_kg<7>(cfg, hdr, tiles, st);
+    case 9: return launch_batch_kg<9>(cfg, hdr, tiles, st);
+    default: return fail(VSR_ERR_UNSUPPORTED, "batch Gaussian size must be odd and <= %d", kBatchMaxKG);
+  }
 }

@@ -165,6 +165,7 @@ int vsr_device_info(int* sm_count, int* cc_major, int* cc_minor) {
 int vsr_tuning_count(int op) {
   switch (op) {
     case VSR_OP_HORN: return vsr::horn_config_count();
+    case VSR_OP_BATCH: return vsr::batch_config_count();
     default: return 0;
   }
 }

@@ -45,6 +45,7 @@ int sm_count();  // cached per device
 // Launch-configuration table chosen by the autotuner (vsr_tuning_set).
 int tuning_get(int op);
 int horn_config_count();
+int batch_config_count();
 
 // ----------------------------------------------------------- dtype traits --
 inline size_t dtype_size(int dt) {

@@ -86,7 +86,8 @@ def build(verbose: bool = False, force: bool = False, ptxas_verbose: bool = Fals
     objs = [BUILD_DIR / (s.stem + ".o") for s in sources]
     if force or jobs or not LIB_PATH.exists() or any(o.stat().st_mtime > LIB_PATH.stat().st_mtime for o in objs):
         tmp = LIB_PATH.with_suffix(".so.tmp")
-        cmd = [nvcc(), GENCODE, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart_static", "-ldl", "-lpthread", "-lrt"]
+        cmd = [nvcc(), GENCODE, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart_static", "-ldl", "-lpthread", "-lrt",
+               "-Xlinker", "--no-undefined"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if verbose or r.returncode:
             sys.stderr.write(f"[vsr build] {' '.join(cmd)}\n{r.stdout}{r.stderr}")

@@ -19,7 +19,7 @@ from pathlib import Path
 from vsr_gb300 import _lib
 
 HORN_CONFIGS = [  # mirrors kHornConfigs in csrc/horn.cu: (rows per tile, stages, threads)
-    (32, 3, 256), (64, 2, 256), (16, 4, 128), (32, 2, 128), (64, 3, 256),
+    (64, 2, 256), (32, 2, 128), (32, 3, 256),
 ]
 
 
