@@ -179,6 +179,14 @@ VSR_API int vsr_gaussian(const void* src, int dtype, int64_t height, int64_t wid
                  int out_dtype, int64_t out_pitch, int precision, void* workspace,
                  size_t workspace_bytes, void* stream);
 
+/* Band-first stacks in ONE launch: ``bands`` rasters ``band_stride`` elements
+ * apart (output bands ``out_band_stride`` apart), otherwise as vsr_gaussian.
+ * Replaces the per-band loop of dispatch_per_band_gpu (dispatch.py:417-506). */
+VSR_API int vsr_gaussian_bands(const void* src, int dtype, int bands, int64_t band_stride, int64_t height,
+                       int64_t width, int64_t pitch, double sigma, int kernel_size, double nodata,
+                       int nodata_kind, void* dst, int out_dtype, int64_t out_band_stride, int64_t out_pitch,
+                       int precision, void* workspace, size_t workspace_bytes, void* stream);
+
 /* ---- focal mean ----------------------------------------------------------
  * Replaces the ``focal_stats`` launch with stat_type 2 (algebra.py:3239-3349,
  * kernel kernels/focal.py:672-769) and the CPU ``_focal_mean_cpu``
@@ -189,6 +197,11 @@ VSR_API int vsr_gaussian(const void* src, int dtype, int64_t height, int64_t wid
 VSR_API int vsr_focal_mean(const void* src, int dtype, int64_t height, int64_t width, int64_t pitch,
                    int radius_y, int radius_x, double nodata, int nodata_kind, void* dst,
                    int out_dtype, int64_t out_pitch, void* stream);
+/* Band-first stacks in one launch (see vsr_gaussian_bands). */
+VSR_API int vsr_focal_mean_bands(const void* src, int dtype, int bands, int64_t band_stride, int64_t height,
+                         int64_t width, int64_t pitch, int radius_y, int radius_x, double nodata,
+                         int nodata_kind, void* dst, int out_dtype, int64_t out_band_stride, int64_t out_pitch,
+                         void* stream);
 
 /* ---- batched tiles: one persistent launch ------------------------------------
  * Many float32 DEM tiles of uneven sizes, each with its own cell size and

@@ -71,6 +71,18 @@ __device__ __forceinline__ float load_elem(const void* base, int dtype, int64_t 
   }
 }
 
+__device__ __forceinline__ int elem_size(int dtype) {
+  return dtype == VSR_U8 ? 1 : (dtype == VSR_I16 || dtype == VSR_U16) ? 2 : (dtype == VSR_F64 ? 8 : 4);
+}
+
+// Base pointer of band blockIdx.z (band-first stacks, ``stride`` elements apart).
+__device__ __forceinline__ const void* band_src(const void* p, int dtype, int64_t stride) {
+  return static_cast<const char*>(p) + static_cast<int64_t>(blockIdx.z) * stride * elem_size(dtype);
+}
+__device__ __forceinline__ void* band_dst(void* p, int out_dtype, int64_t stride) {
+  return static_cast<char*>(p) + static_cast<int64_t>(blockIdx.z) * stride * (out_dtype == VSR_F64 ? 8 : 4);
+}
+
 __device__ __forceinline__ void store_out(void* dst, int out_dtype, int64_t idx, double v) {
   if (out_dtype == VSR_F64) static_cast<double*>(dst)[idx] = v;
   else static_cast<float*>(dst)[idx] = static_cast<float>(v);
@@ -158,6 +170,7 @@ struct ConvArgs {
   void* dst;
   int out_dtype;
   int64_t out_pitch;
+  int64_t band_stride, out_band_stride;  // elements between bands (grid z)
 };
 
 inline size_t conv_smem_bytes(int kh, int kw) {
@@ -217,6 +230,8 @@ __global__ void __launch_bounds__(256) conv_direct(const ConvArgs a) {
   const int64_t x0 = static_cast<int64_t>(blockIdx.x) * kCTW;
   const int64_t y0 = static_cast<int64_t>(blockIdx.y) * kCTH;
   const int px = a.kw / 2, py = a.kh / 2;
+  const void* src = band_src(a.src, a.dtype, a.band_stride);
+  void* dst = band_dst(a.dst, a.out_dtype, a.out_band_stride);
 
   for (int i = tid; i < a.kh * a.kw4; i += 256) wt[i] = a.w32[i];
   bool any_gap = false;
@@ -226,7 +241,7 @@ __global__ void __launch_bounds__(256) conv_direct(const ConvArgs a) {
     float v = 0.0f, d = 0.0f;
     if (gy >= 0 && gy < a.H && gx >= 0 && gx < a.W) {
       bool ok;
-      const float x = load_elem(a.src, a.dtype, gy * a.pitch + gx, a.nd, ok);
+      const float x = load_elem(src, a.dtype, gy * a.pitch + gx, a.nd, ok);
       v = x * (ok ? 1.0f : 0.0f);  // NaN * 0 stays NaN, as in the reference
       d = ok ? 1.0f : 0.0f;
       any_gap |= !ok;
@@ -266,31 +281,31 @@ __global__ void __launch_bounds__(256) conv_direct(const ConvArgs a) {
       const bool centre_ok = vd[(r0 + ry + py) * PW + pos(c0 + rx + px)] != 0.0f;
       const float dn = den[ry][rx];
       const double out = (centre_ok && dn > 0.0f) ? static_cast<double>(num[ry][rx] / dn) : a.nd_out;
-      store_out(a.dst, a.out_dtype, y * a.out_pitch + x, out);
+      store_out(dst, a.out_dtype, y * a.out_pitch + x, out);
     }
   }
 }
 
 template <int MAXW>
-int launch_conv_direct(const ConvArgs& a, cudaStream_t st) {
+int launch_conv_direct(const ConvArgs& a, cudaStream_t st, int bands = 1) {
   const size_t smem = conv_smem_bytes(a.kh, a.kw);
   auto kern = conv_direct<MAXW>;
   VSR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-  dim3 grid(static_cast<unsigned>((a.W + kCTW - 1) / kCTW), static_cast<unsigned>((a.H + kCTH - 1) / kCTH));
+  dim3 grid(static_cast<unsigned>((a.W + kCTW - 1) / kCTW), static_cast<unsigned>((a.H + kCTH - 1) / kCTH), bands);
   if (grid.y > 65535u) return fail(VSR_ERR_UNSUPPORTED, "raster too tall for the direct convolution grid");
   kern<<<grid, dim3(32, 8), smem, st>>>(a);
   VSR_CUDA_TRY(cudaGetLastError());
   return VSR_OK;
 }
 
-int run_conv_direct(const ConvArgs& a, cudaStream_t st) {
-  if (a.kw <= 4) return launch_conv_direct<4>(a, st);
-  if (a.kw <= 8) return launch_conv_direct<8>(a, st);
-  if (a.kw <= 16) return launch_conv_direct<16>(a, st);
-  if (a.kw <= 32) return launch_conv_direct<32>(a, st);
-  if (a.kw <= 48) return launch_conv_direct<48>(a, st);
-  if (a.kw <= 64) return launch_conv_direct<64>(a, st);
-  return launch_conv_direct<80>(a, st);
+int run_conv_direct(const ConvArgs& a, cudaStream_t st, int bands = 1) {
+  if (a.kw <= 4) return launch_conv_direct<4>(a, st, bands);
+  if (a.kw <= 8) return launch_conv_direct<8>(a, st, bands);
+  if (a.kw <= 16) return launch_conv_direct<16>(a, st, bands);
+  if (a.kw <= 32) return launch_conv_direct<32>(a, st, bands);
+  if (a.kw <= 48) return launch_conv_direct<48>(a, st, bands);
+  if (a.kw <= 64) return launch_conv_direct<64>(a, st, bands);
+  return launch_conv_direct<80>(a, st, bands);
 }
 
 constexpr int kMaxDirectK = 80;
@@ -310,6 +325,7 @@ struct SepArgs {
   void* dst;
   int out_dtype;
   int64_t out_pitch;
+  int64_t band_stride, out_band_stride;
 };
 
 inline size_t sep_smem_bytes(int k) {
@@ -331,6 +347,8 @@ __global__ void __launch_bounds__(256) sep_tile(const SepArgs a) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t x0 = static_cast<int64_t>(blockIdx.x) * kSTW;
   const int64_t y0 = static_cast<int64_t>(blockIdx.y) * kSTH;
+  const void* src = band_src(a.src, a.dtype, a.band_stride);
+  void* dst = band_dst(a.dst, a.out_dtype, a.out_band_stride);
 
   for (int i = tid; i < k; i += 256) g[i] = a.g32[i];
   for (int i = tid; i < SH * SW; i += 256) {
@@ -339,7 +357,7 @@ __global__ void __launch_bounds__(256) sep_tile(const SepArgs a) {
     float v = 0.0f, d = 0.0f;
     if (gy >= 0 && gy < a.H && gx >= 0 && gx < a.W) {
       bool ok;
-      const float x = load_elem(a.src, a.dtype, gy * a.pitch + gx, a.nd, ok);
+      const float x = load_elem(src, a.dtype, gy * a.pitch + gx, a.nd, ok);
       v = x * (ok ? 1.0f : 0.0f);
       d = ok ? 1.0f : 0.0f;
     }
@@ -397,17 +415,17 @@ __global__ void __launch_bounds__(256) sep_tile(const SepArgs a) {
       if (y >= a.H) break;
       const bool centre_ok = vd[(q0 + ry + r) * PW + pos(c + r)] != 0.0f;
       const double out = (centre_ok && den[ry] > 0.0f) ? static_cast<double>(num[ry] / den[ry]) : a.nd_out;
-      store_out(a.dst, a.out_dtype, y * a.out_pitch + x, out);
+      store_out(dst, a.out_dtype, y * a.out_pitch + x, out);
     }
   }
 }
 
 template <int MAXK>
-int launch_sep(const SepArgs& a, cudaStream_t st) {
+int launch_sep(const SepArgs& a, cudaStream_t st, int bands = 1) {
   const size_t smem = sep_smem_bytes(a.k);
   auto kern = sep_tile<MAXK>;
   VSR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-  dim3 grid(static_cast<unsigned>((a.W + kSTW - 1) / kSTW), static_cast<unsigned>((a.H + kSTH - 1) / kSTH));
+  dim3 grid(static_cast<unsigned>((a.W + kSTW - 1) / kSTW), static_cast<unsigned>((a.H + kSTH - 1) / kSTH), bands);
   if (grid.y > 65535u) return fail(VSR_ERR_UNSUPPORTED, "raster too tall for the separable Gaussian grid");
   kern<<<grid, 256, smem, st>>>(a);
   VSR_CUDA_TRY(cudaGetLastError());
@@ -415,6 +433,175 @@ int launch_sep(const SepArgs& a, cudaStream_t st) {
 }
 
 constexpr int kMaxSepK = 33;
+
+// ------------------------------------------------------------ sep_strip --
+// Separable Gaussian for large k: a CTA walks a 128-column strip down a
+// segment of rows.  Each input row is reduced along x ONCE (row pass: weighted
+// sums of v*valid and of valid over the kernel width) into a ring of the last
+// k + kSBR - 1 row results in shared memory; every kSBR new rows the column
+// pass combines k ring rows into kSBR output rows.  Work per output pixel is
+// ~4k FMAs (plus k/kSSEG of row-pass halo) instead of 2k^2.
+constexpr int kSTW2 = 128;  // strip width
+constexpr int kSBR = 8;     // rows per step
+constexpr int kSSEG = 512;  // rows per CTA segment
+
+inline size_t strip_smem_bytes(int k) {
+  const int NR = k + kSBR - 1;
+  const int SW = kSTW2 + k - 1;
+  return static_cast<size_t>(2 * NR * kSTW2 + 2 * kSBR * padded_width(SW) + ((k + 3) & ~3)) * 4 + 16;
+}
+
+__global__ void __launch_bounds__(256) sep_strip(const SepArgs a) {
+  extern __shared__ __align__(16) float ssm[];
+  const int k = a.k, r = k / 2;
+  const int NR = k + kSBR - 1;
+  const int SW = kSTW2 + k - 1, PW = padded_width(SW);
+  float* Rn = ssm;                 // NR x kSTW2 ring (numerator)
+  float* Rd = Rn + NR * kSTW2;     // NR x kSTW2 ring (weight sum)
+  float* vz = Rd + NR * kSTW2;     // kSBR x PW staged v*valid
+  float* vd = vz + kSBR * PW;      // kSBR x PW staged valid
+  float* g = vd + kSBR * PW;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t x0 = static_cast<int64_t>(blockIdx.x) * kSTW2;
+  const int64_t ys = static_cast<int64_t>(blockIdx.y) * kSSEG;
+  const int64_t ye = min(ys + kSSEG, a.H);
+  const void* src = band_src(a.src, a.dtype, a.band_stride);
+  void* dst = band_dst(a.dst, a.out_dtype, a.out_band_stride);
+  for (int i = tid; i < ((k + 3) & ~3); i += 256) g[i] = a.g32[i];  // zero padded by the prep kernel
+
+  // Input rows ys - r .. ye + r - 1 pass through the ring; row gy lives in
+  // slot (gy - (ys - r)) % NR.
+  const int64_t first = ys - r;
+  const int64_t last = ye + r;  // exclusive
+  int64_t next_out = ys;
+  for (int64_t rb = first; rb < last; rb += kSBR) {
+    __syncthreads();  // previous column pass is done with the staging rows
+    // stage kSBR input rows (or fewer at the end)
+    for (int i = tid; i < kSBR * SW; i += 256) {
+      const int q = i / SW, c = i - q * SW;
+      const int64_t gy = rb + q, gx = x0 + c - r;
+      float v = 0.0f, d = 0.0f;
+      if (gy < last && gy >= 0 && gy < a.H && gx >= 0 && gx < a.W) {
+        bool ok;
+        const float x = load_elem(src, a.dtype, gy * a.pitch + gx, a.nd, ok);
+        v = x * (ok ? 1.0f : 0.0f);  // NaN * 0 stays NaN, as in the reference
+        d = ok ? 1.0f : 0.0f;
+      }
+      vz[q * PW + pos(c)] = v;
+      vd[q * PW + pos(c)] = d;
+    }
+    __syncthreads();
+    // row pass: warp q handles staged row q, 4 columns per lane; taps are
+    // walked 4 at a time over a 7-value window (no large register arrays)
+    {
+      const int q = warp;
+      const int64_t gy = rb + q;
+      if (gy < last) {
+        const int slot = static_cast<int>((gy - first) % NR);
+        const int c0 = 4 * lane;
+#pragma unroll
+        for (int plane = 0; plane < 2; ++plane) {
+          const float* row = (plane == 0 ? vz : vd) + q * PW;
+          float acc[4] = {};
+          float a0 = row[pos(c0)], a1 = row[pos(c0 + 1)], a2 = row[pos(c0 + 2)];
+          for (int t = 0; t < k; t += 4) {
+            // columns past the staged row are read (inside the buffer) but
+            // never multiplied: taps t+j >= k are skipped
+            const float b0 = row[pos(c0 + t + 3)], b1 = row[pos(c0 + t + 4)];
+            const float b2 = row[pos(c0 + t + 5)], b3 = row[pos(c0 + t + 6)];
+            const float V[7] = {a0, a1, a2, b0, b1, b2, b3};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              if (t + j < k) {
+                const float w = g[t + j];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) acc[u] = fmaf(w, V[u + j], acc[u]);
+              }
+            }
+            a0 = b1;
+            a1 = b2;
+            a2 = b3;
+          }
+          *reinterpret_cast<float4*>((plane == 0 ? Rn : Rd) + slot * kSTW2 + c0) =
+              make_float4(acc[0], acc[1], acc[2], acc[3]);
+        }
+      }
+    }
+    __syncthreads();
+    // column pass for the output rows whose window [y-r, y+r] is now in the
+    // ring (at most kSBR per step): 2 groups of 128 threads, 4 rows each,
+    // taps walked 4 at a time over a 7-row window of the ring
+    const int64_t ready_to = min(rb + kSBR - r, ye);  // outputs y < ready_to are complete
+    if (ready_to > next_out) {
+      const int c = tid & (kSTW2 - 1);
+      const int grp = tid >> 7;
+      const int64_t x = x0 + c;
+      const int64_t yb = next_out + 4 * grp;
+      if (yb < ready_to) {
+        float num[4] = {}, den[4] = {};
+        int sl = static_cast<int>((yb - r - first) % NR);
+        auto nxt = [&](int v) { return v + 1 == NR ? 0 : v + 1; };
+        float an[3], ad[3];
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+          an[m] = Rn[sl * kSTW2 + c];
+          ad[m] = Rd[sl * kSTW2 + c];
+          sl = nxt(sl);
+        }
+        for (int t = 0; t < k; t += 4) {
+          float bn[4], bd[4];
+#pragma unroll
+          for (int m = 0; m < 4; ++m) {
+            // ring slots past the window hold other rows: read, never used
+            bn[m] = Rn[sl * kSTW2 + c];
+            bd[m] = Rd[sl * kSTW2 + c];
+            sl = nxt(sl);
+          }
+          const float Vn[7] = {an[0], an[1], an[2], bn[0], bn[1], bn[2], bn[3]};
+          const float Vd[7] = {ad[0], ad[1], ad[2], bd[0], bd[1], bd[2], bd[3]};
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            if (t + j < k) {
+              const float w = g[t + j];
+#pragma unroll
+              for (int u = 0; u < 4; ++u) {
+                num[u] = fmaf(w, Vn[u + j], num[u]);
+                den[u] = fmaf(w, Vd[u + j], den[u]);
+              }
+            }
+          }
+#pragma unroll
+          for (int m = 0; m < 3; ++m) {
+            an[m] = bn[m + 1];
+            ad[m] = bd[m + 1];
+          }
+        }
+        if (x < a.W) {
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int64_t y = yb + u;
+            if (y >= ready_to) break;
+            bool centre_ok;
+            (void)load_elem(src, a.dtype, y * a.pitch + x, a.nd, centre_ok);
+            const double out = (centre_ok && den[u] > 0.0f) ? static_cast<double>(num[u] / den[u]) : a.nd_out;
+            store_out(dst, a.out_dtype, y * a.out_pitch + x, out);
+          }
+        }
+      }
+      next_out = ready_to;
+    }
+  }
+}
+
+int launch_strip(const SepArgs& a, cudaStream_t st, int bands) {
+  const size_t smem = strip_smem_bytes(a.k);
+  auto kern = sep_strip;
+  VSR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  dim3 grid(static_cast<unsigned>((a.W + kSTW2 - 1) / kSTW2), static_cast<unsigned>((a.H + kSSEG - 1) / kSSEG), bands);
+  kern<<<grid, 256, smem, st>>>(a);
+  VSR_CUDA_TRY(cudaGetLastError());
+  return VSR_OK;
+}
 
 // ------------------------------------------------------------- box_mean --
 // Accumulators: exact int32 sums (<= 16-bit integer rasters), float TwoSum
@@ -461,6 +648,7 @@ struct BoxArgs {
   void* dst;
   int out_dtype;
   int64_t out_pitch;
+  int64_t band_stride, out_band_stride;
 };
 
 template <class Acc>
@@ -500,13 +688,15 @@ __global__ void __launch_bounds__(256) box_mean(const BoxArgs a) {
   const int tid = threadIdx.x;
   const int64_t x0 = static_cast<int64_t>(blockIdx.x) * kBTW;
   const int64_t y0 = static_cast<int64_t>(blockIdx.y) * kBTH;
+  const void* src = band_src(a.src, a.dtype, a.band_stride);
+  void* dst = band_dst(a.dst, a.out_dtype, a.out_band_stride);
 
   for (int i = tid; i < SH * SW; i += 256) {
     const int rr = i / SW, c = i - rr * SW;
     const int64_t gy = y0 + rr - a.ry, gx = x0 + c - a.rx;
     double v = 0.0;
     bool ok = false;
-    if (gy >= 0 && gy < a.H && gx >= 0 && gx < a.W) v = box_load<Acc>(a.src, a.dtype, gy * a.pitch + gx, a.nd, ok);
+    if (gy >= 0 && gy < a.H && gx >= 0 && gx < a.W) v = box_load<Acc>(src, a.dtype, gy * a.pitch + gx, a.nd, ok);
     sv[i] = ok ? v : 0.0;
     sd[i] = ok ? 1 : 0;
   }
@@ -541,20 +731,20 @@ __global__ void __launch_bounds__(256) box_mean(const BoxArgs a) {
     // The reference masks only nodata centres (algebra.py:3099-3100); a NaN
     // centre that is not the nodata value still gets its window mean.
     bool centre_ok = true;
-    if (a.nd.kind != VSR_NODATA_NONE) (void)load_elem(a.src, a.dtype, y * a.pitch + x, a.nd, centre_ok);
+    if (a.nd.kind != VSR_NODATA_NONE) (void)load_elem(src, a.dtype, y * a.pitch + x, a.nd, centre_ok);
     const bool centre_nodata = !centre_ok;
     const double out = (centre_nodata || n == 0) ? a.nd_out : s.value() / static_cast<double>(n);
-    store_out(a.dst, a.out_dtype, y * a.out_pitch + x, out);
+    store_out(dst, a.out_dtype, y * a.out_pitch + x, out);
   }
 }
 
 template <class Acc>
-int launch_box(const BoxArgs& a, cudaStream_t st) {
+int launch_box(const BoxArgs& a, cudaStream_t st, int bands = 1) {
   const size_t smem = box_smem_bytes<Acc>(a.ry, a.rx);
   if (smem > 227 * 1024) return fail(VSR_ERR_UNSUPPORTED, "focal mean radius (%d, %d) too large", a.ry, a.rx);
   auto kern = box_mean<Acc>;
   VSR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-  dim3 grid(static_cast<unsigned>((a.W + kBTW - 1) / kBTW), static_cast<unsigned>((a.H + kBTH - 1) / kBTH));
+  dim3 grid(static_cast<unsigned>((a.W + kBTW - 1) / kBTW), static_cast<unsigned>((a.H + kBTH - 1) / kBTH), bands);
   if (grid.y > 65535u) return fail(VSR_ERR_UNSUPPORTED, "raster too tall for the focal mean grid");
   kern<<<grid, 256, smem, st>>>(a);
   VSR_CUDA_TRY(cudaGetLastError());
@@ -664,11 +854,12 @@ extern "C" size_t vsr_gaussian_workspace_size(int kernel_size, int precision) {
   return gauss_ws(k);
 }
 
-extern "C" int vsr_gaussian(const void* src, int dtype, int64_t height, int64_t width, int64_t pitch, double sigma,
-                            int kernel_size, double nodata, int nodata_kind, void* dst, int out_dtype,
-                            int64_t out_pitch, int precision, void* workspace, size_t workspace_bytes,
-                            void* stream) {
+static int gaussian_impl(const void* src, int dtype, int bands, int64_t band_stride, int64_t height, int64_t width,
+                         int64_t pitch, double sigma, int kernel_size, double nodata, int nodata_kind, void* dst,
+                         int out_dtype, int64_t out_band_stride, int64_t out_pitch, int precision, void* workspace,
+                         size_t workspace_bytes, void* stream) {
   if (!(sigma > 0.0)) return fail(VSR_ERR_INVALID_ARG, "sigma must be positive, got %g", sigma);
+  if (bands < 1) return fail(VSR_ERR_INVALID_ARG, "bands must be >= 1");
   int rc = check_raster(src, dtype, height, width, pitch, dst, out_dtype, out_pitch);
   if (rc || height == 0 || width == 0) return rc;
   if (precision < VSR_PREC_AUTO || precision > VSR_PREC_SPLIT_BF16) return fail(VSR_ERR_INVALID_ARG, "bad precision %d", precision);
@@ -682,36 +873,64 @@ extern "C" int vsr_gaussian(const void* src, int dtype, int64_t height, int64_t 
   const int k4 = (k + 3) & ~3;
   char* ws = static_cast<char*>(workspace);
   float* g32 = reinterpret_cast<float*>(ws);
-  float* w2 = reinterpret_cast<float*>(ws + ((static_cast<size_t>(k4) * 4 + 255) & ~size_t(255)));
-  float* wsum = reinterpret_cast<float*>(ws + need - 256);
-  const bool separable = k <= kMaxSepK;
-  prep_gaussian<<<1, 256, k * sizeof(double), st>>>(k, k4, sigma, g32, separable ? nullptr : w2, wsum);
+  prep_gaussian<<<1, 256, k * sizeof(double), st>>>(k, k4, sigma, g32, nullptr, nullptr);
   VSR_CUDA_TRY(cudaGetLastError());
   const NodataSpec nd = make_nodata(dtype, nodata, nodata_kind);
-  if (separable) {
-    SepArgs a{src, dtype, height, width, pitch, nd, g32, k, nodata, dst, out_dtype, out_pitch};
-    if (k <= 8) return launch_sep<8>(a, st);
-    if (k <= 16) return launch_sep<16>(a, st);
-    return launch_sep<33>(a, st);
-  }
-  ConvArgs a{src, dtype, height, width, pitch, nd, w2, wsum, k, k, k4, nodata, dst, out_dtype, out_pitch};
-  return run_conv_direct(a, st);
+  SepArgs a{src, dtype, height, width, pitch, nd, g32, k, nodata, dst, out_dtype, out_pitch, band_stride,
+            out_band_stride};
+  if (k <= 8) return launch_sep<8>(a, st, bands);
+  if (k <= 16) return launch_sep<16>(a, st, bands);
+  if (k <= 33) return launch_sep<33>(a, st, bands);
+  return launch_strip(a, st, bands);
 }
 
-extern "C" int vsr_focal_mean(const void* src, int dtype, int64_t height, int64_t width, int64_t pitch,
-                              int radius_y, int radius_x, double nodata, int nodata_kind, void* dst, int out_dtype,
-                              int64_t out_pitch, void* stream) {
+extern "C" int vsr_gaussian(const void* src, int dtype, int64_t height, int64_t width, int64_t pitch, double sigma,
+                            int kernel_size, double nodata, int nodata_kind, void* dst, int out_dtype,
+                            int64_t out_pitch, int precision, void* workspace, size_t workspace_bytes,
+                            void* stream) {
+  return gaussian_impl(src, dtype, 1, 0, height, width, pitch, sigma, kernel_size, nodata, nodata_kind, dst,
+                       out_dtype, 0, out_pitch, precision, workspace, workspace_bytes, stream);
+}
+
+extern "C" int vsr_gaussian_bands(const void* src, int dtype, int bands, int64_t band_stride, int64_t height,
+                                  int64_t width, int64_t pitch, double sigma, int kernel_size, double nodata,
+                                  int nodata_kind, void* dst, int out_dtype, int64_t out_band_stride,
+                                  int64_t out_pitch, int precision, void* workspace, size_t workspace_bytes,
+                                  void* stream) {
+  return gaussian_impl(src, dtype, bands, band_stride, height, width, pitch, sigma, kernel_size, nodata, nodata_kind,
+                       dst, out_dtype, out_band_stride, out_pitch, precision, workspace, workspace_bytes, stream);
+}
+
+static int focal_mean_impl(const void* src, int dtype, int bands, int64_t band_stride, int64_t height,
+                           int64_t width, int64_t pitch, int radius_y, int radius_x, double nodata, int nodata_kind,
+                           void* dst, int out_dtype, int64_t out_band_stride, int64_t out_pitch, void* stream) {
+  if (bands < 1) return fail(VSR_ERR_INVALID_ARG, "bands must be >= 1");
   int rc = check_raster(src, dtype, height, width, pitch, dst, out_dtype, out_pitch);
   if (rc || height == 0 || width == 0) return rc;
   if (radius_y < 0 || radius_x < 0) return fail(VSR_ERR_INVALID_ARG, "radius must be non-negative");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   BoxArgs a{src, dtype, height, width, pitch, make_nodata(dtype, nodata, nodata_kind), radius_y, radius_x,
-            nodata, dst, out_dtype, out_pitch};
+            nodata, dst, out_dtype, out_pitch, band_stride, out_band_stride};
   switch (dtype) {
     case VSR_U8:
     case VSR_I16:
-    case VSR_U16: return launch_box<AccI>(a, st);
-    case VSR_F32: return launch_box<AccF2>(a, st);
-    default: return launch_box<AccD>(a, st);
+    case VSR_U16: return launch_box<AccI>(a, st, bands);
+    case VSR_F32: return launch_box<AccF2>(a, st, bands);
+    default: return launch_box<AccD>(a, st, bands);
   }
+}
+
+extern "C" int vsr_focal_mean(const void* src, int dtype, int64_t height, int64_t width, int64_t pitch,
+                              int radius_y, int radius_x, double nodata, int nodata_kind, void* dst, int out_dtype,
+                              int64_t out_pitch, void* stream) {
+  return focal_mean_impl(src, dtype, 1, 0, height, width, pitch, radius_y, radius_x, nodata, nodata_kind, dst,
+                         out_dtype, 0, out_pitch, stream);
+}
+
+extern "C" int vsr_focal_mean_bands(const void* src, int dtype, int bands, int64_t band_stride, int64_t height,
+                                    int64_t width, int64_t pitch, int radius_y, int radius_x, double nodata,
+                                    int nodata_kind, void* dst, int out_dtype, int64_t out_band_stride,
+                                    int64_t out_pitch, void* stream) {
+  return focal_mean_impl(src, dtype, bands, band_stride, height, width, pitch, radius_y, radius_x, nodata,
+                         nodata_kind, dst, out_dtype, out_band_stride, out_pitch, stream);
 }

@@ -77,6 +77,14 @@ SIGNATURES: dict[str, tuple] = {
     "vsr_batch_plan_size": (_sz, [_int]),
     "vsr_batch_plan": (_int, [_vp, _int, _dbl, _int, _vp, _sz, _c.POINTER(_c.c_int64), _vp]),
     "vsr_batch_run": (_int, [_vp, _int, _vp]),
+    "vsr_gaussian_bands": (
+        _int,
+        [_vp, _int, _int, _i64, _i64, _i64, _i64, _dbl, _int, _dbl, _int, _vp, _int, _i64, _i64, _int, _vp, _sz, _vp],
+    ),
+    "vsr_focal_mean_bands": (
+        _int,
+        [_vp, _int, _int, _i64, _i64, _i64, _i64, _int, _int, _dbl, _int, _vp, _int, _i64, _i64, _vp],
+    ),
     "vsr_focal_mean": (
         _int,
         [_vp, _int, _i64, _i64, _i64, _int, _int, _dbl, _int, _vp, _int, _i64, _vp],

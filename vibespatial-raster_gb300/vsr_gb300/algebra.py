@@ -370,12 +370,11 @@ def gaussian_bands(raster: OwnedRasterArray, sigma: float, kernel_size: int | No
     nbytes = lib.vsr_gaussian_workspace_size(k, prec)
     ws = _workspace(nbytes, src.device)
     stream = _stream_handle()
-    esz, osz = src.element_size(), dst.element_size()
-    for b in range(B):
-        st = lib.vsr_gaussian(src.data_ptr() + b * H * W * esz, _lib.dtype_code(dt), H, W, W, float(sigma), k,
-                              nd_out if kind == _lib.VSR_NODATA_VALUE else ndv, kind,
-                              dst.data_ptr() + b * H * W * osz, ocode, W, prec, _aligned_ptr(ws), nbytes, stream)
-        _lib.check(st, "vsr_gaussian")
+    # all bands in one launch (band-first stack, H*W elements apart)
+    st = lib.vsr_gaussian_bands(src.data_ptr(), _lib.dtype_code(dt), B, H * W, H, W, W, float(sigma), k,
+                                nd_out if kind == _lib.VSR_NODATA_VALUE else ndv, kind, dst.data_ptr(), ocode,
+                                H * W, W, prec, _aligned_ptr(ws), nbytes, stream)
+    _lib.check(st, "vsr_gaussian_bands")
     return dst
 
 
@@ -411,12 +410,10 @@ def focal_mean_bands(raster: OwnedRasterArray, ry: int, rx: int, *, out_dtype=np
     dst = out if out is not None else torch.empty((B, H, W), dtype=torch_dtype(odt), device=src.device)
     lib = _lib.load()
     stream = _stream_handle()
-    esz, osz = src.element_size(), dst.element_size()
-    for b in range(B):
-        st = lib.vsr_focal_mean(src.data_ptr() + b * H * W * esz, _lib.dtype_code(dt), H, W, W, ry, rx,
-                                nd_out if kind == _lib.VSR_NODATA_VALUE else ndv, kind,
-                                dst.data_ptr() + b * H * W * osz, ocode, W, stream)
-        _lib.check(st, "vsr_focal_mean")
+    st = lib.vsr_focal_mean_bands(src.data_ptr(), _lib.dtype_code(dt), B, H * W, H, W, W, ry, rx,
+                                  nd_out if kind == _lib.VSR_NODATA_VALUE else ndv, kind, dst.data_ptr(), ocode,
+                                  H * W, W, stream)
+    _lib.check(st, "vsr_focal_mean_bands")
     return dst
 
 
