@@ -10,8 +10,9 @@ needed between steps.
 
 Prints ONE JSON line (rank 0).  ``value`` is device throughput (Gpixel/s) with
 the DEM resident in HBM; ``e2e`` is the same metric through the public API
-(from_numpy of a pinned host DEM -> raster_terrain -> to_numpy into pinned
-host buffers), copies included.  ``--impl reference`` times the reference's
+(from_numpy of a pinned host DEM -> raster_terrain_host into pinned host
+buffers: row strips streamed through the GPU with the copies overlapped),
+copies included.  ``--impl reference`` times the reference's
 CPU algorithm (the float64 numpy restatement in oracle/, the reference being
 pure Python) on the host cores.  Under torchrun each rank runs its own
 replica (the path shards by raster; no collective on the data path).
@@ -241,12 +242,13 @@ def run_vsr(args, ws, rank, local):
     in_np = host_in.numpy()
     out_np = [t.numpy() for t in host_out]
 
+    from vsr_gb300 import stream as vstream
+
     def e2e_step():
+        # public API, host in -> host out: row strips streamed through the GPU
+        # with host->device, kernel and device->host overlapped on 3 streams
         rr = vsr.from_numpy(in_np, nodata=dem.nodata, affine=dem.affine)
-        res = vsr.raster_terrain(rr)
-        res["slope"].to_numpy(out=out_np[0])
-        res["aspect"].to_numpy(out=out_np[1])
-        res["hillshade"].to_numpy(out=out_np[2])
+        vstream.raster_terrain_host(rr, out=out_np)
 
     e2e_step()
     torch.cuda.synchronize()

@@ -476,19 +476,23 @@ __global__ void __launch_bounds__(256) sep_strip(const SepArgs a) {
   int64_t next_out = ys;
   for (int64_t rb = first; rb < last; rb += kSBR) {
     __syncthreads();  // previous column pass is done with the staging rows
-    // stage kSBR input rows (or fewer at the end)
-    for (int i = tid; i < kSBR * SW; i += 256) {
-      const int q = i / SW, c = i - q * SW;
-      const int64_t gy = rb + q, gx = x0 + c - r;
-      float v = 0.0f, d = 0.0f;
-      if (gy < last && gy >= 0 && gy < a.H && gx >= 0 && gx < a.W) {
-        bool ok;
-        const float x = load_elem(src, a.dtype, gy * a.pitch + gx, a.nd, ok);
-        v = x * (ok ? 1.0f : 0.0f);  // NaN * 0 stays NaN, as in the reference
-        d = ok ? 1.0f : 0.0f;
+    // stage kSBR input rows (or fewer at the end): warp q takes row q
+    {
+      const int q = warp;
+      const int64_t gy = rb + q;
+      const bool row_in = gy < last && gy >= 0 && gy < a.H;
+      for (int c = lane; c < SW; c += 32) {
+        const int64_t gx = x0 + c - r;
+        float v = 0.0f, d = 0.0f;
+        if (row_in && gx >= 0 && gx < a.W) {
+          bool ok;
+          const float x = load_elem(src, a.dtype, gy * a.pitch + gx, a.nd, ok);
+          v = x * (ok ? 1.0f : 0.0f);  // NaN * 0 stays NaN, as in the reference
+          d = ok ? 1.0f : 0.0f;
+        }
+        vz[q * PW + pos(c)] = v;
+        vd[q * PW + pos(c)] = d;
       }
-      vz[q * PW + pos(c)] = v;
-      vd[q * PW + pos(c)] = d;
     }
     __syncthreads();
     // row pass: warp q handles staged row q, 4 columns per lane; taps are
@@ -751,6 +755,168 @@ int launch_box(const BoxArgs& a, cudaStream_t st, int bands = 1) {
   return VSR_OK;
 }
 
+// -------------------------------------------------------- box_mean_fast --
+// Focal mean for <= 16-bit integer (exact int32 sums) and float32 (TwoSum
+// float pairs) rasters.  A 128 x 32 output tile is staged as values (0 where
+// invalid) plus a byte count plane; the row pass slides a (2rx+1)-wide
+// window along runs of 16 columns (add the entering value, subtract the
+// leaving one: exact for integers, compensated for floats), the column pass
+// slides a (2ry+1)-tall window down 16-row runs.  mean = sum / count.
+constexpr int kFTW = 128, kFTH = 32, kFRun = 16;
+
+template <bool FLOAT>
+struct FastSum;
+template <>
+struct FastSum<false> {
+  int32_t s;
+  __device__ void zero() { s = 0; }
+  // integer rasters are staged as int32 bit patterns in the value plane
+  __device__ void add(float v) { s += __float_as_int(v); }
+  __device__ void sub(float v) { s -= __float_as_int(v); }
+  __device__ void add(const FastSum& o) { s += o.s; }
+  __device__ void sub(const FastSum& o) { s -= o.s; }
+  __device__ double value() const { return static_cast<double>(s); }
+};
+template <>
+struct FastSum<true> {
+  float s, c;
+  __device__ void zero() { s = 0.0f; c = 0.0f; }
+  __device__ void two_sum(float v) {
+    const float t = s + v;
+    const float bp = t - s;
+    c += (s - (t - bp)) + (v - bp);
+    s = t;
+  }
+  __device__ void add(float v) { two_sum(v); }
+  __device__ void sub(float v) { two_sum(-v); }
+  __device__ void add(const FastSum& o) { two_sum(o.s); c += o.c; }
+  __device__ void sub(const FastSum& o) { two_sum(-o.s); c -= o.c; }
+  __device__ double value() const { return static_cast<double>(s) + static_cast<double>(c); }
+};
+
+constexpr int kFRS = kFTW + 1;  // odd row stride of the row-sum planes (no bank conflicts)
+constexpr int kMaxFastWindow = 1023;  // windows up to 1023 taps use the fast kernel
+
+template <bool FLOAT>
+inline size_t box_fast_smem(int ry, int rx) {
+  const int SH = kFTH + 2 * ry, SWp = (kFTW + 2 * rx) | 1;
+  return static_cast<size_t>(SH) * SWp * 5 + static_cast<size_t>(SH) * kFRS * (sizeof(FastSum<FLOAT>) + 4) + 64;
+}
+
+template <bool FLOAT>
+__global__ void __launch_bounds__(256) box_mean_fast(const BoxArgs a) {
+  using Sum = FastSum<FLOAT>;
+  extern __shared__ __align__(16) unsigned char fraw[];
+  const int SH = kFTH + 2 * a.ry, SW = kFTW + 2 * a.rx, SWp = SW | 1;  // odd stride: rows in distinct banks
+  const int wx = 2 * a.rx + 1, wy = 2 * a.ry + 1;
+  Sum* rs = reinterpret_cast<Sum*>(fraw);                      // SH x kFRS row sums (8-byte aligned first)
+  float* sv = reinterpret_cast<float*>(rs + SH * kFRS);        // SH x SWp values (0 where invalid)
+  int32_t* rc = reinterpret_cast<int32_t*>(sv + SH * SWp);     // SH x kFRS row counts
+  uint8_t* sd = reinterpret_cast<uint8_t*>(rc + SH * kFRS);    // SH x SWp valid
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t x0 = static_cast<int64_t>(blockIdx.x) * kFTW;
+  const int64_t y0 = static_cast<int64_t>(blockIdx.y) * kFTH;
+  const void* src = band_src(a.src, a.dtype, a.band_stride);
+  void* dst = band_dst(a.dst, a.out_dtype, a.out_band_stride);
+  // 1/n for every possible count (float32 outputs)
+  __shared__ float inv_n[kMaxFastWindow + 1];
+  for (int i = tid; i <= wx * wy && i <= kMaxFastWindow; i += 256) inv_n[i] = i ? 1.0f / static_cast<float>(i) : 0.0f;
+
+  for (int rr = warp; rr < SH; rr += 8) {
+    const int64_t gy = y0 + rr - a.ry;
+    const bool row_in = gy >= 0 && gy < a.H;
+    for (int c = lane; c < SW; c += 32) {
+      const int64_t gx = x0 + c - a.rx;
+      float v = 0.0f;
+      bool ok = false;
+      if (row_in && gx >= 0 && gx < a.W) {
+        v = load_elem(src, a.dtype, gy * a.pitch + gx, a.nd, ok);
+        ok = ok && (v == v);  // NaN never counts (the CPU reference excludes it)
+      }
+      // float rasters: the value; integer rasters: its int32 bit pattern
+      sv[rr * SWp + c] = FLOAT ? (ok ? v : 0.0f) : __int_as_float(ok ? static_cast<int32_t>(v) : 0);
+      sd[rr * SWp + c] = ok ? 1 : 0;
+    }
+  }
+  __syncthreads();
+  // row pass: units (row, 16-column run); consecutive lanes take consecutive rows
+  const int runs_x = kFTW / kFRun;
+  for (int u = tid; u < SH * runs_x; u += 256) {
+    const int rr = u % SH, c0 = (u / SH) * kFRun;
+    const float* row = sv + rr * SWp + c0;
+    const uint8_t* drow = sd + rr * SWp + c0;
+    Sum sum;
+    sum.zero();
+    int n = 0;
+    for (int t = 0; t < wx; ++t) {
+      sum.add(row[t]);
+      n += drow[t];
+    }
+    rs[rr * kFRS + c0] = sum;
+    rc[rr * kFRS + c0] = n;
+    for (int j = 1; j < kFRun; ++j) {
+      sum.add(row[j + wx - 1]);
+      sum.sub(row[j - 1]);
+      n += static_cast<int>(drow[j + wx - 1]) - static_cast<int>(drow[j - 1]);
+      rs[rr * kFRS + c0 + j] = sum;
+      rc[rr * kFRS + c0 + j] = n;
+    }
+  }
+  __syncthreads();
+  // column pass: one column, a run of 16 rows per thread
+  const int c = tid & (kFTW - 1);
+  const int64_t x = x0 + c;
+  for (int q0 = (tid >> 7) * kFRun; q0 < kFTH; q0 += 2 * kFRun) {
+    Sum sum;
+    sum.zero();
+    int n = 0;
+    for (int t = 0; t < wy; ++t) {
+      sum.add(rs[(q0 + t) * kFRS + c]);
+      n += rc[(q0 + t) * kFRS + c];
+    }
+    for (int j = 0; j < kFRun; ++j) {
+      if (j > 0) {
+        sum.add(rs[(q0 + j + wy - 1) * kFRS + c]);
+        sum.sub(rs[(q0 + j - 1) * kFRS + c]);
+        n += rc[(q0 + j + wy - 1) * kFRS + c] - rc[(q0 + j - 1) * kFRS + c];
+      }
+      const int64_t y = y0 + q0 + j;
+      if (y >= a.H || x >= a.W) continue;
+      // nodata centre: the reference masks only nodata (not NaN) centres
+      bool centre_ok = true;
+      if (a.nd.kind != VSR_NODATA_NONE && !sd[(q0 + j + a.ry) * SWp + c + a.rx]) {
+        bool ok;
+        (void)load_elem(src, a.dtype, y * a.pitch + x, a.nd, ok);
+        centre_ok = ok;
+      }
+      double out;
+      if (!centre_ok || n == 0) {
+        out = a.nd_out;
+      } else if (a.out_dtype == VSR_F64) {
+        out = sum.value() / static_cast<double>(n);
+      } else {
+        // float32 output: one multiply by the count's reciprocal (<= 1 ulp)
+        out = FLOAT ? static_cast<double>(static_cast<float>(sum.value()) * inv_n[n])
+                    : static_cast<double>(static_cast<float>(sum.s) * inv_n[n]);
+      }
+      store_out(dst, a.out_dtype, y * a.out_pitch + x, out);
+    }
+  }
+}
+
+template <bool FLOAT>
+int launch_box_fast(const BoxArgs& a, cudaStream_t st, int bands) {
+  const size_t smem = box_fast_smem<FLOAT>(a.ry, a.rx);
+  if (smem > 227 * 1024) return fail(VSR_ERR_UNSUPPORTED, "focal mean radius (%d, %d) too large", a.ry, a.rx);
+  auto kern = box_mean_fast<FLOAT>;
+  VSR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  dim3 grid(static_cast<unsigned>((a.W + kFTW - 1) / kFTW), static_cast<unsigned>((a.H + kFTH - 1) / kFTH), bands);
+  if (grid.y > 65535u) return fail(VSR_ERR_UNSUPPORTED, "raster too tall for the focal mean grid");
+  kern<<<grid, 256, smem, st>>>(a);
+  VSR_CUDA_TRY(cudaGetLastError());
+  return VSR_OK;
+}
+
 // ------------------------------------------------------- shared checks --
 int check_raster(const void* src, int dtype, int64_t H, int64_t W, int64_t pitch, const void* dst,
                  int out_dtype, int64_t out_pitch) {
@@ -914,8 +1080,13 @@ static int focal_mean_impl(const void* src, int dtype, int bands, int64_t band_s
   switch (dtype) {
     case VSR_U8:
     case VSR_I16:
-    case VSR_U16: return launch_box<AccI>(a, st, bands);
-    case VSR_F32: return launch_box<AccF2>(a, st, bands);
+    case VSR_U16:
+      // int32 sums stay exact for windows of <= 1023 16-bit values
+      if ((2 * radius_y + 1) * (2 * radius_x + 1) <= kMaxFastWindow) return launch_box_fast<false>(a, st, bands);
+      return launch_box<AccD>(a, st, bands);
+    case VSR_F32:
+      if ((2 * radius_y + 1) * (2 * radius_x + 1) <= kMaxFastWindow) return launch_box_fast<true>(a, st, bands);
+      return launch_box<AccF2>(a, st, bands);
     default: return launch_box<AccD>(a, st, bands);
   }
 }

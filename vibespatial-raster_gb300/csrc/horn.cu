@@ -637,6 +637,7 @@ struct BatchTileDev {
   int64_t first_item;  // prefix sum of items over earlier tiles
   int64_t items_x;     // blocks across this tile
   int32_t vec;         // outputs 16-byte aligned with pitch % 4 == 0
+  float inv8cx, inv8cy;  // 1 / (8 cell), formed in FP64 on the device at plan time
   int32_t pad_;
 };
 
@@ -658,6 +659,8 @@ struct BatchSmem {
   static constexpr int kFloats = SR * kSW + 2 * SR * kTW;
 };
 
+constexpr int kBatchSmemTiles = 2048;  // tiles whose prefix sums are searched in shared memory
+
 template <int TH, int THREADS, int KG>
 __global__ void __launch_bounds__(THREADS) batch_terrain_kernel(BatchHeader* __restrict__ hdr,
                                                                 const BatchTileDev* __restrict__ tiles) {
@@ -670,6 +673,7 @@ __global__ void __launch_bounds__(THREADS) batch_terrain_kernel(BatchHeader* __r
   float* S = bsm;                 // SR x kSW staged values
   float* Rn = S + SR * kSW;       // SR x kTW row-pass numerator
   float* Rd = Rn + SR * kTW;      // SR x kTW row-pass weight sum
+  __shared__ int64_t sh_first[kBatchSmemTiles];
   __shared__ int64_t sh_item;
   __shared__ int sh_tile;
   __shared__ HornParams sh_P;
@@ -677,35 +681,48 @@ __global__ void __launch_bounds__(THREADS) batch_terrain_kernel(BatchHeader* __r
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t total = hdr->total_items;
   const int n_tiles = hdr->n_tiles;
+  const bool smem_search = n_tiles <= kBatchSmemTiles;
+  if (smem_search)
+    for (int i = tid; i < n_tiles; i += THREADS) sh_first[i] = tiles[i].first_item;
+  int cur_tile = -1;
+  // the next item is claimed one step ahead, so the atomic's latency overlaps
+  // the current item's work
+  int64_t next_item = 0;
+  if (tid == 0) next_item = static_cast<int64_t>(atomicAdd(&hdr->counter, 1ull));
+  __syncthreads();
 
   for (;;) {
     if (tid == 0) {
-      const int64_t item = static_cast<int64_t>(atomicAdd(&hdr->counter, 1ull));
+      const int64_t item = next_item;
       sh_item = item;
       if (item < total) {
+        next_item = static_cast<int64_t>(atomicAdd(&hdr->counter, 1ull));
         int lo = 0, hi = n_tiles - 1;  // last tile with first_item <= item
         while (lo < hi) {
           const int mid = (lo + hi + 1) >> 1;
-          if (tiles[mid].first_item <= item) lo = mid;
+          const int64_t f = smem_search ? sh_first[mid] : tiles[mid].first_item;
+          if (f <= item) lo = mid;
           else hi = mid - 1;
         }
         sh_tile = lo;
-        const BatchTileDev& T = tiles[lo];
-        HornParams P{};
-        P.height = T.H;
-        P.width = T.W;
-        P.in_pitch = T.pitch;
-        P.out_pitch = T.out_pitch;
-        P.hs_pitch = T.out_pitch;
-        // per-tile cell-size scale formed in FP64 on the device
-        P.inv8cx = static_cast<float>(1.0 / (8.0 * T.cell_x));
-        P.inv8cy = static_cast<float>(1.0 / (8.0 * T.cell_y));
-        P.nd_out_f = static_cast<float>(T.nodata);
-        P.nd_out_d = T.nodata;
-        P.flags = T.flags;
-        P.nd_kind = T.nd_kind;
-        sh_P = P;
-        sh_nd = static_cast<float>(T.nodata);
+        if (lo != cur_tile) {  // consecutive items usually share a tile
+          cur_tile = lo;
+          const BatchTileDev& T = tiles[lo];
+          HornParams P{};
+          P.height = T.H;
+          P.width = T.W;
+          P.in_pitch = T.pitch;
+          P.out_pitch = T.out_pitch;
+          P.hs_pitch = T.out_pitch;
+          P.inv8cx = T.inv8cx;
+          P.inv8cy = T.inv8cy;
+          P.nd_out_f = static_cast<float>(T.nodata);
+          P.nd_out_d = T.nodata;
+          P.flags = T.flags;
+          P.nd_kind = T.nd_kind;
+          sh_P = P;
+          sh_nd = static_cast<float>(T.nodata);
+        }
       }
     }
     __syncthreads();
@@ -714,20 +731,26 @@ __global__ void __launch_bounds__(THREADS) batch_terrain_kernel(BatchHeader* __r
     const BatchTileDev& T = tiles[sh_tile];
     const HornParams P = sh_P;
     const float nd_in = sh_nd;
-    const int64_t local = item - T.first_item;
-    const int64_t by = local / T.items_x, bx = local - by * T.items_x;
+    const int64_t local = item - (smem_search ? sh_first[sh_tile] : T.first_item);
+    const int64_t items_x = (P.width + kTW - 1) / kTW;
+    const int64_t by = local / items_x, bx = local - by * items_x;
     const int64_t x0 = bx * kTW, y0 = by * TH;
-    const int64_t H = T.H, W = T.W;
+    const int64_t H = P.height, W = P.width;
+    const float* srcp = T.src;
 
-    // Stage rows y0-HY .. y0+TH+HY-1, columns x0-4 .. x0+131 (clamped).
+    // Stage rows y0-HY .. y0+TH+HY-1, columns x0-4 .. x0+131 (clamped), one
+    // warp per row, lanes along the row (coalesced for any pitch).
     bool any_nd = false;
-    for (int i = tid; i < SR * kSW; i += THREADS) {
-      const int r = i / kSW, c = i - r * kSW;
+    for (int r = warp; r < SR; r += WARPS) {
       const int64_t gy = min(max(y0 - HY + r, int64_t(0)), H - 1);
-      const int64_t gx = min(max(x0 - 4 + c, int64_t(0)), W - 1);
-      const float v = __ldg(T.src + gy * T.pitch + gx);
-      S[i] = v;
-      any_nd |= is_nd(v, P.nd_kind, nd_in);
+      const float* rowp = srcp + gy * P.in_pitch;
+#pragma unroll
+      for (int c = lane; c < kSW; c += 32) {
+        const int64_t gx = min(max(x0 - 4 + c, int64_t(0)), W - 1);
+        const float v = __ldg(rowp + gx);
+        S[r * kSW + c] = v;
+        any_nd |= is_nd(v, P.nd_kind, nd_in);
+      }
     }
     const bool masked = __syncthreads_or(any_nd);
     const bool edge = x0 + kTW > W || y0 + TH > H;
@@ -846,6 +869,15 @@ int launch_batch_kg(int cfg, BatchHeader* hdr, const BatchTileDev* tiles, cudaSt
   }
 }
 
+// Per-tile 1 / (8 cell) in FP64 on the device (the cell sizes come from each
+// tile's affine transform).
+__global__ void prep_batch_cells(BatchTileDev* tiles, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  tiles[i].inv8cx = static_cast<float>(1.0 / (8.0 * tiles[i].cell_x));
+  tiles[i].inv8cy = static_cast<float>(1.0 / (8.0 * tiles[i].cell_y));
+}
+
 __global__ void prep_batch_gauss(BatchHeader* hdr, int kg, double sigma) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   double s = 0.0;
@@ -910,6 +942,7 @@ extern "C" int vsr_batch_plan(const vsr_batch_tile* tiles_host, int n_tiles, dou
     d.nd_kind = resolve_nodata(VSR_F32, t.nodata, t.nodata_kind, &ev);
     d.flags = t.flags;
     d.vec = (!t.slope || (aligned(t.slope, 16) && aligned(t.aspect, 16))) && t.out_pitch % 4 == 0;
+    d.inv8cx = d.inv8cy = 0.0f;  // set on the device by prep_batch_cells
     d.pad_ = 0;
     d.items_x = (t.width + kTW - 1) / kTW;
     d.first_item = items;
@@ -927,6 +960,8 @@ extern "C" int vsr_batch_plan(const vsr_batch_tile* tiles_host, int n_tiles, dou
   const size_t off = (sizeof(BatchHeader) + 255) & ~size_t(255);
   VSR_CUDA_TRY(cudaMemcpyAsync(base, &h, sizeof(h), cudaMemcpyHostToDevice, st));
   VSR_CUDA_TRY(cudaMemcpyAsync(base + off, dev.data(), dev.size() * sizeof(BatchTileDev), cudaMemcpyHostToDevice, st));
+  prep_batch_cells<<<(n_tiles + 127) / 128, 128, 0, st>>>(reinterpret_cast<BatchTileDev*>(base + off), n_tiles);
+  VSR_CUDA_TRY(cudaGetLastError());
   if (gauss_k) {
     prep_batch_gauss<<<1, 32, 0, st>>>(reinterpret_cast<BatchHeader*>(base), gauss_k, sigma);
     VSR_CUDA_TRY(cudaGetLastError());

@@ -1,0 +1,140 @@
+"""Streamed host-to-host terrain pass: row strips with a halo, copies overlapped.
+
+The GB300 counterpart of the reference's out-of-core tiling
+(``dispatch_tiled_halo``, src/vibespatial/raster/tiling.py:468-659, with its
+halo/affine rules at :564-579) for the fused Horn pass.  The DEM stays in
+host memory (ideally page-locked); it is cut into row strips that carry a
+one-row halo above and below, and each strip goes through
+
+    host -> device copy  |  vsr_horn_fused on the strip  |  device -> host copy
+
+on its own CUDA stream, round-robin over ``n_streams`` streams, so the
+copy engines (one per direction) and the SMs work on different strips at
+the same time.  Output rows of a strip are taken from its inner rows, whose
+neighbours are real data; the raster's own first and last rows keep the
+reference's edge replication.  Results are identical to ``raster_terrain``
+on the whole raster.
+"""
+
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from vsr_gb300 import _lib
+from vsr_gb300.algebra import NODATA_CENTER, NODATA_WINDOW, cellsize, nodata_kind
+from vsr_gb300.buffers import OwnedRasterArray, from_numpy
+
+
+def _pinned_view(a: np.ndarray):
+    import torch
+
+    t = torch.from_numpy(a)
+    return t, bool(t.is_pinned())
+
+
+def terrain_host(dem: np.ndarray, affine, nodata, *, slope_out: np.ndarray | None = None,
+                 aspect_out: np.ndarray | None = None, hs_out: np.ndarray | None = None,
+                 azimuth: float = 315.0, altitude: float = 45.0, z_factor: float = 1.0,
+                 nodata_mode: str = NODATA_WINDOW, strip_rows: int = 1024, n_streams: int = 3):
+    """Fill the given host arrays (float32 slope/aspect, uint8 hillshade) from a host DEM."""
+    import torch
+
+    if dem.ndim != 2 or dem.dtype != np.float32:
+        raise ValueError("terrain_host streams single-band float32 DEMs")
+    H, W = dem.shape
+    outs = [o for o in (slope_out, aspect_out, hs_out)]
+    for o, dt in zip(outs, (np.float32, np.float32, np.uint8)):
+        if o is not None and (o.shape != (H, W) or o.dtype != dt or not o.flags.c_contiguous):
+            raise ValueError("outputs must be C-contiguous (H, W) arrays: float32 slope/aspect, uint8 hillshade")
+    if slope_out is None and aspect_out is None and hs_out is None:
+        return
+    lib = _lib.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    src_t, _ = _pinned_view(np.ascontiguousarray(dem))
+    host_outs = [torch.from_numpy(o) if o is not None else None for o in outs]
+    kind = nodata_kind(OwnedRasterArray(data=dem, nodata=nodata, dtype=dem.dtype, affine=tuple(affine)))[0]
+    ndv = float(nodata) if nodata is not None else 0.0
+    if kind == _lib.VSR_NODATA_NAN:
+        ndv = float("nan")
+    flags = _lib.VSR_HORN_CENTER_ONLY if nodata_mode == NODATA_CENTER else _lib.VSR_HORN_SA_NAN_UNMASKED
+    cx, cy = cellsize(affine)
+    zen = math.radians(90.0 - float(altitude))
+    az = math.radians(float(azimuth))
+    sr = max(1, min(int(strip_rows), H))
+    cap = sr + 2
+    streams = [torch.cuda.Stream(device=dev) for _ in range(n_streams)]
+    bufs = []
+    for _ in range(n_streams):
+        bufs.append((
+            torch.empty((cap, W), dtype=torch.float32, device=dev),
+            torch.empty((cap, W), dtype=torch.float32, device=dev) if slope_out is not None else None,
+            torch.empty((cap, W), dtype=torch.float32, device=dev) if aspect_out is not None else None,
+            torch.empty((cap, W), dtype=torch.uint8, device=dev) if hs_out is not None else None,
+        ))
+    cur = torch.cuda.current_stream(dev)
+    for s in streams:
+        s.wait_stream(cur)  # buffers were allocated on the current stream
+    n_strips = (H + sr - 1) // sr
+    for i in range(n_strips):
+        y0, y1 = i * sr, min(H, (i + 1) * sr)
+        lo, hi = max(0, y0 - 1), min(H, y1 + 1)  # strip with its halo rows
+        rows = hi - lo
+        s = streams[i % n_streams]
+        d_in, d_s, d_a, d_h = bufs[i % n_streams]
+        with torch.cuda.stream(s):
+            d_in[:rows].copy_(src_t[lo:hi], non_blocking=True)
+            st = lib.vsr_horn_fused(
+                d_in.data_ptr(), _lib.VSR_F32, rows, W, W, cx, cy, ndv, kind, flags,
+                d_s.data_ptr() if d_s is not None else None, d_a.data_ptr() if d_a is not None else None,
+                _lib.VSR_F32, W, d_h.data_ptr() if d_h is not None else None, W, float(z_factor), zen, az,
+                s.cuda_stream)
+            _lib.check(st, "vsr_horn_fused")
+            a, b = y0 - lo, y1 - lo  # inner rows of the strip
+            for d, h in zip((d_s, d_a, d_h), host_outs):
+                if d is not None:
+                    h[y0:y1].copy_(d[a:b], non_blocking=True)
+    for s in streams:
+        cur.wait_stream(s)
+    cur.synchronize()
+
+
+def raster_terrain_host(dem: OwnedRasterArray, *, slope: bool = True, aspect: bool = True, hillshade: bool = True,
+                        azimuth: float = 315.0, altitude: float = 45.0, z_factor: float = 1.0,
+                        nodata_mode: str = NODATA_WINDOW, out=None, strip_rows: int = 1024,
+                        n_streams: int = 3) -> dict[str, OwnedRasterArray]:
+    """``raster_terrain`` for a host-resident DEM with host-resident results.
+
+    Streams row strips through the GPU (copies overlapped with the fused
+    kernel) instead of copying the whole raster in and out; works for DEMs
+    larger than device memory.  ``out`` may give preallocated host arrays
+    (slope, aspect, hillshade) -- page-locked ones make the copies
+    asynchronous.
+    """
+    z = dem.to_numpy()
+    if z.ndim == 3:
+        if z.shape[0] != 1:
+            raise ValueError("raster_terrain_host streams single-band DEMs")
+        z = z[0]
+    H, W = z.shape
+    o_s, o_a, o_h = out if out is not None else (None, None, None)
+    if slope and o_s is None:
+        o_s = np.empty((H, W), np.float32)
+    if aspect and o_a is None:
+        o_a = np.empty((H, W), np.float32)
+    if hillshade and o_h is None:
+        o_h = np.empty((H, W), np.uint8)
+    terrain_host(np.asarray(z, dtype=np.float32), dem.affine, dem.nodata, slope_out=o_s if slope else None,
+                 aspect_out=o_a if aspect else None, hs_out=o_h if hillshade else None, azimuth=azimuth,
+                 altitude=altitude, z_factor=z_factor, nodata_mode=nodata_mode, strip_rows=strip_rows,
+                 n_streams=n_streams)
+    res = {}
+    if slope:
+        res["slope"] = from_numpy(o_s, nodata=dem.nodata, affine=dem.affine, crs=dem.crs)
+    if aspect:
+        res["aspect"] = from_numpy(o_a, nodata=dem.nodata, affine=dem.affine, crs=dem.crs)
+    if hillshade:
+        res["hillshade"] = from_numpy(o_h, nodata=0 if dem.nodata is not None else None, affine=dem.affine,
+                                      crs=dem.crs)
+    return res
