@@ -359,8 +359,10 @@ def run_conv(args, ws, rank, local):
             for _ in range(max(3, args.warmup)):
                 fn()
             t[prec] = _time_ms(fn, args.steps, stream)
-        kp = ((16 + k - 1) + 15) // 16 * 16
-        issued = 3 * 2 * H * W * k * kp / 16  # 3 split MMAs, K = kp per kernel row, N = 16 per tile
+        kp = ((64 + k - 1) + 15) // 16 * 16
+        # 3 split products per kernel row; a 128 x 64 output tile multiplies
+        # K = kp (window width rounded to 16): 2 * kp flops per output per row
+        issued = 3 * 2 * H * W * k * kp
         res[name] = {"k": k, "fp32_ms": t["fp32"], "split_bf16_ms": t["split_bf16"],
                      "speedup": t["fp32"] / t["split_bf16"],
                      "fp32_gpix_s": H * W / t["fp32"] / 1e6, "split_bf16_gpix_s": H * W / t["split_bf16"] / 1e6,

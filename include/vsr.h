@@ -152,7 +152,7 @@ VSR_API int vsr_convolve(const void* src, int dtype, int64_t height, int64_t wid
  * boundary (ctypes / cgo / JNI) without the process allocator, or work issued
  * while a CUDA graph capture forbids allocation.  Same arguments and results
  * as vsr_convolve without the workspace: the scratch is a static device
- * array inside libvsr (108,288 bytes, enough for kernels up to 80 x 80,
+ * array inside libvsr (248,320 bytes, enough for kernels up to 80 x 80,
  * held by every GPU that loads the library until the process exits).
  * Kernels larger than 80 x 80 are rejected with VSR_ERR_UNSUPPORTED.  The
  * first call on each device resolves the array's device address (with that

@@ -1,37 +1,50 @@
 // Split-BF16 tcgen05 implicit GEMM for large normalised focal convolutions.
 //
-// Formulation (one output tile = 128 image rows x N image columns):
+// Formulation (one output tile = 128 image rows x 64 image columns):
 //   out[y0+m, x0+n] = sum_ky sum_k' X[m+ky][k'] * w[ky][k'-n]
-// where X is the tile's input window (128+kh-1 rows x N+kw-1 columns).  For
+// where X is the tile's input window (128+kh-1 rows x 64+kw-1 columns).  For
 // each kernel row ky this is a GEMM  C[m][n] += A_ky[m][k'] B_ky[k'][n]  with
 // A_ky = X shifted down ky rows and B_ky the Toeplitz band of weight row ky.
 //
 // Operand layouts (canonical K-major, no swizzle: 8-row x 16-byte core
 // matrices, LBO = stride between core matrices along K, SBO = along M/N):
 //  * A is stored with its K index reversed (k = Kp-1-k') and rows 16 bytes
-//    apart, so A_ky is the same descriptor advanced by ky*16 bytes -- no copy
-//    per kernel row.
+//    apart, so A_ky is the same descriptor advanced by ky*16 bytes.
 //  * B (also K-reversed) satisfies B[n+8][k-8] = B[n][k]; with SBO = LBO =
 //    128 bytes every (n-group, k-chunk) pair maps to core matrix n/8 + k/8,
-//    so a kernel row's Toeplitz band needs only (Kp/8 + N/8 - 1) core
-//    matrices of shared memory.
-// Precision: values are centred on the tile's centre pixel (mu) and split
-// z = z_hi + z_lo, w = w_hi + w_lo (BF16); num = z_hi w_hi + z_hi w_lo +
-// z_lo w_hi accumulates in FP32 in tensor memory.  The weight sum comes from
-// the same split weights (a 0/1 validity operand times w_hi and w_lo), so the
-// quotient is a consistently weighted average; out = num/den + mu.
-// NaN taps (the reference's NaN * 0 poisoning) and +-inf are excluded from
-// the GEMM and their window footprint is marked NaN from per-row bitmasks.
+//    so one kernel row's Toeplitz band is Kp/8 + 64/8 - 1 core matrices.
+// Tile width: a tcgen05.mma with M = 128 costs a fixed ~51 cycles up to
+// N = 64 and runs at the full rate only from N = 128
+// (diagnostics/mma_issue_probe.cu); with the Toeplitz padding (N + kw - 1
+// taps of K per N outputs) N = 64 and N = 128 cost the same per output and
+// N = 64 needs half the shared memory.
 //
-// Pipeline per persistent CTA (128 threads, one CTA per SM):
-//   TMA 2-D load of the tile window -> all threads convert to BF16 hi/lo and
-//   validity in the MMA layout -> the next tile's TMA is issued -> thread 0
-//   issues the tcgen05.mma chains and commits to an mbarrier; the epilogue of
-//   the previous tile (tcgen05.ld of its accumulators, FP32 sums, stores)
-//   runs while the tensor core works on this one (two A-operand buffers when
-//   they fit, two TMEM buffers).
-// Every wait is bounded (an error code in the device word on expiry; the
-// CTA then frees its tensor memory and leaves).
+// Precision: values are centred on the tile's centre pixel (mu) and split
+// z = z_hi + z_lo, w = w_hi + w_lo (BF16).  The hi*hi chain accumulates in
+// FP32 tensor memory in groups of kernel rows (the accumulation error grows
+// with the number of MMAs chained into one accumulator), the two correction
+// products (hi*lo, lo*hi) in one more accumulator; the groups are added in
+// FP32 registers.  The weight sum uses the same split weights, so the
+// quotient is a consistently weighted mean: on tiles whose window holds no
+// nodata it comes from a summed-area table of w_hi + w_lo (borders only
+// clip the window), otherwise from a 0/1 validity operand times w_hi and
+// w_lo.  out = num/den + mu.  NaN taps (the reference's NaN * valid
+// poisoning) and +-inf are kept out of the GEMM; per-row bitmasks give
+// their window footprints: NaN, or the infinite sum the reference forms.
+//
+// Persistent CTA, one per SM, 6 warps with fixed roles:
+//   warp 0      issues the tcgen05.mma chains of each tile
+//   warp 1      streams the Toeplitz bands, one kernel row per stage, into a
+//               shared-memory ring with cp.async.bulk
+//   warps 2..5  convert the next tile's window to BF16 hi/lo (+ validity) in
+//               the MMA layout straight from global memory, then run the
+//               previous tile's epilogue (tcgen05.ld, FP32 sums, stores)
+// The roles hand over through mbarriers: full/empty pairs for the A buffers
+// (two when they fit), the TMEM accumulator buffers (two when they fit) and
+// the band ring.  Every wait is bounded: on expiry the waiter records an
+// error code and raises a shared abort flag that ends the other roles'
+// waits; the MMA issuer and the band producer then wait (bounded) for their
+// own operations in flight before the CTA frees its tensor memory.
 #include <cuda_bf16.h>
 
 #include "vsr_internal.cuh"
@@ -46,20 +59,25 @@ int run_conv_tc(const void* src, int dtype, int64_t H, int64_t W, int64_t pitch,
 
 namespace {
 
-constexpr int kM = 128;     // output rows per tile (TMEM lanes)
-constexpr int kTN = 16;     // output columns per tile (MMA N)
-constexpr int kThreadsTC = 256;
+constexpr int kM = 128;            // output rows per tile (TMEM lanes, MMA M)
+constexpr int kTN = 64;            // output columns per tile (MMA N)
+constexpr int kConvWarps = 8;      // warps 2..9
+constexpr int kConvThreads = 32 * kConvWarps;
+constexpr int kThreadsTC = 64 + kConvThreads;
 constexpr int kMaxTCK = 41;
+constexpr int kStages = 8;         // Toeplitz band ring depth
+constexpr int kConvRows = 6;       // window rows a converter warp loads per batch
 
 struct TcGeom {
   int kh, kw;
-  int R;       // staged rows = kM + kh - 1
-  int KW;      // useful window width = kTN + kw - 1
-  int Kp;      // GEMM K (KW rounded up to 16)
-  int KC;      // Kp / 8 core-matrix columns
-  int KS;      // Kp / 16 MMA k-steps
-  int NB;      // core matrices per Toeplitz band = KC + kTN/8 - 1
-  int BW;      // TMA box width (floats), 16-byte multiple covering KW + 3
+  int R;   // window rows = kM + kh - 1
+  int Rp;  // A operand: 16-byte rows between core-matrix columns (odd: conflict-free 8-byte stores)
+  int KW;  // window columns = kTN + kw - 1
+  int Kp;  // GEMM K per kernel row (KW rounded up to 16)
+  int KC;  // Kp / 8 core-matrix columns
+  int KS;  // Kp / 16 MMA k-steps
+  int NB;  // core matrices per Toeplitz band = KC + kTN/8 - 1
+  int G;   // hi*hi (and weight-sum) accumulator groups
 };
 
 __host__ __device__ inline TcGeom make_geom(int kh, int kw) {
@@ -67,58 +85,83 @@ __host__ __device__ inline TcGeom make_geom(int kh, int kw) {
   g.kh = kh;
   g.kw = kw;
   g.R = kM + kh - 1;
+  g.Rp = g.R | 1;
   g.KW = kTN + kw - 1;
   g.Kp = (g.KW + 15) & ~15;
   g.KC = g.Kp / 8;
   g.KS = g.Kp / 16;
   g.NB = g.KC + kTN / 8 - 1;
-  g.BW = (g.KW + 3 + 3) & ~3;
+  // MMAs per output that touch non-zero weights: kh rows x the k-steps a
+  // kw-wide band overlaps; at most ~64 of them per accumulator.
+  const int chain = kh * ((kw + 15) / 16 + 1);
+  g.G = chain <= 64 ? 1 : (chain <= 128 ? 2 : 3);
   return g;
 }
 
-struct TcSmem {  // byte offsets inside the 1024-aligned dynamic shared memory
-  uint32_t a_hi, a_lo, a_valid, a_stride, bw, stage, ctr, nanrow, total;
+struct TcPlan {  // shared-memory byte offsets (1024-aligned base) and pipeline shape
+  uint32_t a_bytes;             // one operand buffer
+  uint32_t a_hi, a_lo, a_vd;    // nbuf buffers each
+  uint32_t ring, stage_bytes;   // kStages x (hi band, lo band)
+  uint32_t sat;                 // (kh+1) x (kw+1) doubles
+  uint32_t ctr;                 // 2 x kM u64 centre-validity bits
+  uint32_t nanrow;              // 2 x R unsigned __int128 NaN footprints
+  uint32_t infrow;              // 2 x R unsigned __int128 +-inf footprints
+  uint32_t okrow;               // 2 x R unsigned __int128 validity masks (nodata rules)
+  uint32_t total;
+  int nbuf;                     // A buffers (1 or 2)
+  int cols;                     // TMEM columns per accumulator buffer
+  int tbuf;                     // TMEM accumulator buffers (1 or 2)
 };
 
-// nbuf A-operand buffers (2: the next tile is converted while the tensor core
-// works on the current one; 1 when two do not fit).
-__host__ __device__ inline TcSmem make_smem(const TcGeom& g, int nbuf) {
-  TcSmem s;
-  const uint32_t a_bytes = (static_cast<uint32_t>(g.KC) * g.R * 16 + 127) & ~127u;
-  s.a_stride = a_bytes;  // between buffers of one operand
-  s.a_hi = 0;
-  s.a_lo = s.a_hi + nbuf * a_bytes;
-  s.a_valid = s.a_lo + nbuf * a_bytes;
-  s.bw = s.a_valid + nbuf * a_bytes;
-  const uint32_t b_bytes = static_cast<uint32_t>(g.kh) * 2 * g.NB * 128;
-  s.stage = (s.bw + b_bytes + 1023) & ~1023u;
-  const uint32_t stage_bytes = static_cast<uint32_t>(g.R) * g.BW * 4;
-  s.ctr = (s.stage + stage_bytes + 127) & ~127u;
-  s.nanrow = (s.ctr + 2 * kM * kTN + 127) & ~127u;
-  s.total = s.nanrow + 2 * static_cast<uint32_t>(g.R) * 8;
-  return s;
+__host__ __device__ inline TcPlan make_plan(const TcGeom& g, bool has_nd, int nbuf) {
+  TcPlan p;
+  p.nbuf = nbuf;
+  p.a_bytes = (static_cast<uint32_t>(g.KC) * g.Rp * 16 + 127) & ~127u;
+  p.a_hi = 0;
+  p.a_lo = p.a_hi + nbuf * p.a_bytes;
+  p.a_vd = p.a_lo + nbuf * p.a_bytes;
+  p.ring = p.a_vd + (has_nd ? nbuf * p.a_bytes : 0u);
+  p.stage_bytes = 2u * g.NB * 128;
+  p.sat = p.ring + kStages * p.stage_bytes;
+  p.ctr = (p.sat + static_cast<uint32_t>(g.kh + 1) * (g.kw + 1) * 8 + 127) & ~127u;
+  p.nanrow = p.ctr + 2 * kM * 8;
+  p.infrow = p.nanrow + 2 * static_cast<uint32_t>(g.R) * 16;
+  p.okrow = p.infrow + 2 * static_cast<uint32_t>(g.R) * 16;
+  p.total = p.okrow + (has_nd ? 2 * static_cast<uint32_t>(g.R) * 16 : 0u);
+  p.cols = (g.G + 1 + (has_nd ? g.G : 0)) * kTN;  // hh groups | corrections | weight-sum groups
+  p.tbuf = 2 * p.cols <= 512 ? 2 : 1;
+  return p;
 }
 
 // --- tcgen05 / descriptor helpers (PTX ISA: tcgen05 family, sm_100a+) ---
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-  // start address, leading byte offset, stride byte offset (all >> 4),
-  // descriptor version 1 (bits 46-47), no swizzle (bits 61-63 = 0).
-  return (static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4)) |
-         (static_cast<uint64_t>((lbo & 0x3FFFFu) >> 4) << 16) |
-         (static_cast<uint64_t>((sbo & 0x3FFFFu) >> 4) << 32) | (1ull << 46);
-}
+// Shared-memory matrix descriptor: start address, leading byte offset,
+// stride byte offset (all >> 4), version 1 (bits 46-47), no swizzle.
 
 // Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major,
 // M = 128, N = kTN.
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(kTN >> 3) << 17) |
                             (static_cast<uint32_t>(kM >> 4) << 24);
 
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+// Shared-memory descriptors are passed as their two 32-bit halves: the low
+// word holds the start address (>> 4) and the leading byte offset, so
+// stepping an operand is one 32-bit add (addresses stay below 256 KB: the
+// start field never carries); the high word (stride byte offset, version)
+// is the same for every operand here.
+__host__ __device__ constexpr uint32_t desc_lo(uint32_t saddr, uint32_t lbo) {
+  return ((saddr & 0x3FFFFu) >> 4) | (((lbo & 0x3FFFFu) >> 4) << 16);
+}
+constexpr uint32_t kDescHi = (128u >> 4) | (1u << 14);  // SBO = 128 B, version 1 (bit 46)
+
+// The MMA issue loop is latency-bound on one thread: keep it to a handful
+// of instructions per MMA.
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint32_t a_lo, uint32_t b_lo, uint32_t accumulate) {
   asm volatile(
-      "{\n\t.reg .pred p;\n\t"
+      "{\n\t.reg .pred p;\n\t.reg .b64 da, db;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-      ::"r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate));
+      "mov.b64 da, {%1, %5};\n\t"
+      "mov.b64 db, {%2, %5};\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], da, db, %3, p;\n\t}"
+      ::"r"(d_tmem), "r"(a_lo), "r"(b_lo), "r"(kIdesc), "r"(accumulate), "r"(kDescHi));
 }
 
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
@@ -140,15 +183,88 @@ __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// 8 consecutive f32 columns of this warp's 32 TMEM lanes.
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float v[8]) {
-  uint32_t r[8];
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-               : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+// Bulk global -> shared copy completing on ``bar`` (16-byte aligned, size % 16 == 0).
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Bounded wait that also gives up once another role has raised ``abort``.
+__device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, volatile int* abort, uint32_t* err,
+                                              uint32_t code) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_timer_ns();
+  while (!mbar_try_wait(bar, parity)) {
+    if (*abort) return false;
+    if (global_timer_ns() - t0 > kWaitLimitNs) {
+      atomicOr(err, code);
+      *abort = 1;
+      return false;
+    }
+  }
+  return true;
+}
+
+// Named barrier 1 over the converter warps; conv_any also ORs a predicate.
+__device__ __forceinline__ void conv_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kConvThreads) : "memory"); }
+
+__device__ __forceinline__ bool conv_any(bool p) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred q, o;\n\t"
+      "setp.ne.u32 q, %1, 0;\n\t"
+      "bar.red.or.pred o, 1, %2, q;\n\t"
+      "selp.u32 %0, 1, 0, o;\n\t}"
+      : "=r"(r)
+      : "r"(static_cast<uint32_t>(p)), "n"(kConvThreads)
+      : "memory");
+  return r != 0;
+}
+
+// Bit l of b[q] flags window column 4l + q (lane l holds columns 4l..4l+3);
+// returns word w of the column-major mask (columns 32w..32w+31).
+__device__ __forceinline__ uint32_t interleave4(const uint32_t b[4], int w) {
+  uint32_t out = 0;
 #pragma unroll
-  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+  for (int q = 0; q < 4; ++q) {
+    uint32_t x = (b[q] >> (8 * w)) & 0xFFu;  // lanes 8w..8w+7
+    x = (x | (x << 12)) & 0x000F000Fu;
+    x = (x | (x << 6)) & 0x03030303u;
+    x = (x | (x << 3)) & 0x11111111u;  // bit i -> bit 4i
+    out |= x << q;
+  }
+  return out;
+}
+
+struct TcArgs {
+  const float* src;
+  int64_t H, W, pitch;
+  int nd_kind;
+  float nd_f;
+  double nd_out;
+  void* dst;
+  int out_dtype;
+  int64_t out_pitch;
+  int vec_out;                  // float32 output with 16-byte aligned rows
+  const unsigned char* bw_img;  // per kernel row: hi band, lo band (NB core matrices each)
+  const double* sat;            // (kh+1) x (kw+1) prefix sums of w_hi + w_lo
+  const double* w64;            // the kernel as given (windows holding +-inf)
+  int kh, kw;
+  int nbuf;
+};
+
+__device__ __forceinline__ int64_t clamp64(int64_t v, int64_t lo, int64_t hi) {
+  return v < lo ? lo : (v > hi ? hi : v);
+}
+
+__device__ __forceinline__ uint32_t bf16x2_bits(__nv_bfloat162 v) {
+  return static_cast<uint32_t>(__bfloat16_as_ushort(v.x)) | (static_cast<uint32_t>(__bfloat16_as_ushort(v.y)) << 16);
 }
 
 // 16 consecutive f32 columns of this warp's 32 TMEM lanes.
@@ -164,317 +280,483 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16]) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-struct TcNodata {
-  int kind;
-  float fv;
-};
-
-struct TcArgs {
-  int64_t H, W;
-  TcNodata nd;
-  double nd_out;
-  void* dst;
-  int out_dtype;
-  int64_t out_pitch;
-  const uint4* bw_img;  // kh x 2 x NB core matrices (bf16) from the prep kernel
-  const float* wsum;    // sum of (w_hi + w_lo) over all taps
-  int kh, kw;
-  int nbuf;             // A-operand buffers (1 or 2)
-};
-
-__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
-  const __nv_bfloat16 ha = __float2bfloat16_rn(a), hb = __float2bfloat16_rn(b);
-  return static_cast<uint32_t>(__bfloat16_as_ushort(ha)) | (static_cast<uint32_t>(__bfloat16_as_ushort(hb)) << 16);
+// Output of a window that holds +-inf values (and no NaN): the reference
+// sums v * w, so each valid infinite tap adds +-inf (NaN for a zero weight)
+// and the sum is +-inf, or NaN when both signs meet.  Scans the window; such
+// windows are rare.
+__device__ __noinline__ float inf_window(const float* __restrict__ src, int64_t H, int64_t W, int64_t pitch,
+                                         const double* __restrict__ w64, int kh, int kw, int nd_kind, float nd_f,
+                                         int64_t y, int64_t x) {
+  bool pos = false, neg = false, nan = false;
+  for (int ky = 0; ky < kh; ++ky) {
+    const int64_t yy = y + ky - kh / 2;
+    if (yy < 0 || yy >= H) continue;
+    for (int kx = 0; kx < kw; ++kx) {
+      const int64_t xx = x + kx - kw / 2;
+      if (xx < 0 || xx >= W) continue;
+      const float v = __ldg(src + yy * pitch + xx);
+      if (!isinf(v) || (nd_kind == VSR_NODATA_VALUE && v == nd_f)) continue;
+      const double t = static_cast<double>(v) * w64[ky * kw + kx];
+      pos |= t > 0.0;
+      neg |= t < 0.0;
+      nan |= t != t;
+    }
+  }
+  if (nan || (pos && neg)) return __int_as_float(0x7fc00000);
+  return pos ? __int_as_float(0x7f800000) : __int_as_float(0xff800000);
 }
 
-// Accumulators per TMEM buffer (192 columns): hi*hi groups at [0, 64), the
-// correction terms at [64, 80), weight-sum groups at [96, 160).  Each group
-// takes at most ~64 MMAs: tensor-core accumulation error grows with the
-// number of MMAs chained into one accumulator.
-__host__ __device__ inline int tc_groups(int kh, int ks) {
-  const int g = (kh * ks + 63) / 64;
-  return g < 1 ? 1 : (g > 4 ? 4 : g);
-}
-
-__global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const __grid_constant__ CUtensorMap tmap,
-                                                                 const TcArgs a, uint32_t* err_word) {
+// ND: the raster's nodata rule (0 none, 1 a value, 2 NaN).
+template <int ND>
+__global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, uint32_t* err_word) {
   extern __shared__ unsigned char tc_raw[];
-  __shared__ __align__(8) uint64_t tma_bar, mma_bar[2];
+  __shared__ __align__(8) uint64_t a_full[2], a_empty[2], acc_full[2], acc_empty[2], b_full[kStages],
+      b_empty[kStages], drain_bar;
   __shared__ uint32_t tmem_slot;
+  __shared__ volatile int abort_flag;
   __shared__ int64_t info_x0[2], info_y0[2];
   __shared__ float info_mu[2];
-  __shared__ int info_inv[2], info_nan[2];
+  __shared__ int info_nan[2], info_inf[2], info_nd[2];
   unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tc_raw) + 1023) & ~uintptr_t(1023));
   const TcGeom g = make_geom(a.kh, a.kw);
-  const TcSmem L = make_smem(g, a.nbuf);
+  const TcPlan L = make_plan(g, ND != 0, a.nbuf);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t tiles_x = (a.W + kTN - 1) / kTN;
   const int64_t total = tiles_x * ((a.H + kM - 1) / kM);
   const uint32_t s_base = smem_u32(sm);
-  float* stage = reinterpret_cast<float*>(sm + L.stage);
-  const int G = tc_groups(a.kh, g.KS);
-  const uint32_t cols_per_buf = 192;  // hh groups | corr | den groups
+  double* sat = reinterpret_cast<double*>(sm + L.sat);
 
-  // Weight Toeplitz images -> shared memory (once per CTA).
-  {
-    uint4* dstw = reinterpret_cast<uint4*>(sm + L.bw);
-    const int n16 = a.kh * 2 * g.NB * 8;
-    for (int i = tid; i < n16; i += kThreadsTC) dstw[i] = a.bw_img[i];
-  }
-  __shared__ float s_wsum;
-  if (tid == 0) s_wsum = *a.wsum;
-  if (warp == 0) tmem_alloc(&tmem_slot, 512);
+  // ---- set-up: zero the A buffers (K-padding columns stay zero for good),
+  // copy the summed-area table, initialise barriers, allocate tensor memory
+  for (uint32_t i = tid * 16; i < L.ring; i += kThreadsTC * 16)
+    *reinterpret_cast<uint4*>(sm + i) = make_uint4(0u, 0u, 0u, 0u);
+  for (int i = tid; i < (a.kh + 1) * (a.kw + 1); i += kThreadsTC) sat[i] = a.sat[i];
   if (tid == 0) {
-    prefetch_tensormap(&tmap);
-    mbar_init(&tma_bar, 1);
-    mbar_init(&mma_bar[0], 1);
-    mbar_init(&mma_bar[1], 1);
+    abort_flag = 0;
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&a_full[i], kConvThreads);
+      mbar_init(&a_empty[i], 1);
+      mbar_init(&acc_full[i], 1);
+      mbar_init(&acc_empty[i], kConvThreads);
+    }
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&b_full[s], 1);
+      mbar_init(&b_empty[s], 1);
+    }
+    mbar_init(&drain_bar, 1);
     fence_mbar_init();
   }
+  if (warp == 0) tmem_alloc(&tmem_slot, 512);
   fence_proxy_async_smem();
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
-  const uint32_t stage_bytes = static_cast<uint32_t>(g.R) * g.BW * 4;
-  const uint32_t lbo_a = static_cast<uint32_t>(g.R) * 16;
 
-  auto window_x = [&](int64_t t, int64_t& gx0, int64_t& xs) {
-    const int64_t tx = t % tiles_x;
-    gx0 = tx * kTN - a.kw / 2;
-    xs = gx0 >= 0 ? (gx0 & ~int64_t(3)) : -((-gx0 + 3) & ~int64_t(3));
-  };
-  auto issue = [&](int64_t t) {
-    int64_t gx0, xs;
-    window_x(t, gx0, xs);
-    mbar_arrive_expect_tx(&tma_bar, stage_bytes);
-    tma_load_2d(stage, &tmap, static_cast<int>(xs), static_cast<int>((t / tiles_x) * kM - a.kh / 2), &tma_bar);
-  };
-
-  // Epilogue of the tile whose accumulators sit in TMEM buffer tb.
-  auto epilogue = [&](int tb) {
-    const int64_t x0 = info_x0[tb], y0 = info_y0[tb];
-    const float mu = info_mu[tb];
-    const int quarter = warp & 3, half = warp >> 2;  // lanes 32q.., columns 8h..
-    const int m = quarter * 32 + lane;
-    const uint32_t base = tmem + tb * cols_per_buf + (static_cast<uint32_t>(quarter * 32) << 16) + half * 8;
-    float num[8], part[8], den[8];
-    tmem_ld8(base, num);
-    for (int gi = 1; gi < G; ++gi) {
-      tmem_ld8(base + gi * kTN, part);
-#pragma unroll
-      for (int n = 0; n < 8; ++n) num[n] += part[n];
-    }
-    tmem_ld8(base + 64, part);  // correction terms
-#pragma unroll
-    for (int n = 0; n < 8; ++n) num[n] += part[n];
-    if (info_inv[tb]) {
-      tmem_ld8(base + 96, den);
-      for (int gi = 1; gi < G; ++gi) {
-        tmem_ld8(base + 96 + gi * kTN, part);
-#pragma unroll
-        for (int n = 0; n < 8; ++n) den[n] += part[n];
-      }
-    } else {
-#pragma unroll
-      for (int n = 0; n < 8; ++n) den[n] = s_wsum;
-    }
-    const uint8_t* ctr = sm + L.ctr + tb * (kM * kTN);
-    const unsigned long long* nanrow = reinterpret_cast<const unsigned long long*>(sm + L.nanrow) + tb * g.R;
-    unsigned long long nanfoot = 0ull;
-    if (info_nan[tb])
-      for (int j = 0; j < a.kh; ++j) nanfoot |= nanrow[m + j];
-    const int64_t y = y0 + m;
-    if (y < a.H) {
-#pragma unroll
-      for (int n8 = 0; n8 < 8; ++n8) {
-        const int n = half * 8 + n8;
-        const int64_t x = x0 + n;
-        if (x >= a.W) break;
-        double out;
-        if (!ctr[m * kTN + n] || !(den[n8] > 0.0f)) out = a.nd_out;
-        else if ((nanfoot >> n) & 1ull) out = __int_as_float(0x7fc00000);
-        else out = static_cast<double>(num[n8] / den[n8] + mu);
-        if (a.out_dtype == VSR_F64) static_cast<double*>(a.dst)[y * a.out_pitch + x] = out;
-        else static_cast<float*>(a.dst)[y * a.out_pitch + x] = static_cast<float>(out);
-      }
-    }
-  };
-
-  if (tid == 0 && static_cast<int64_t>(blockIdx.x) < total) issue(blockIdx.x);
-
-  uint32_t tma_phase = 0;
-  uint32_t mma_phase[2] = {0u, 0u};
-  bool failed = false;
-  int it = 0;
-  bool prev_pending = false;  // an MMA batch whose epilogue has not run yet
-  for (int64_t t = blockIdx.x; t < total; t += gridDim.x, ++it) {
-    const int b = it % a.nbuf, tb = it & 1;
-    if (a.nbuf == 1 && prev_pending) {
-      // single A buffer: the previous tile's MMAs must finish before it is rewritten
-      const bool done = mbar_wait_bounded(&mma_bar[tb ^ 1], mma_phase[tb ^ 1], err_word, kDevErrMmaTimeout);
-      if (__syncthreads_or(!done)) { failed = true; break; }
-    }
-    const bool ok = mbar_wait_bounded(&tma_bar, tma_phase, err_word, kDevErrTmaTimeout);
-    tma_phase ^= 1;
-    if (__syncthreads_or(!ok)) { failed = true; break; }
-    const int64_t ty = t / tiles_x;
-    int64_t gx0, xs;
-    window_x(t, gx0, xs);
-    const int64_t x0 = (t % tiles_x) * kTN, y0 = ty * kM;
-    const int off = static_cast<int>(gx0 - xs);
-    const int64_t gy0 = y0 - a.kh / 2;
-    float mu = 0.0f;
-    {
-      const int rc = g.R / 2, kc = g.KW / 2;
-      const int64_t yy = gy0 + rc, xx = gx0 + kc;
-      const float v = stage[rc * g.BW + off + kc];
-      const bool valid = yy >= 0 && yy < a.H && xx >= 0 && xx < a.W &&
-                         !(a.nd.kind == VSR_NODATA_VALUE ? v == a.nd.fv : (a.nd.kind == VSR_NODATA_NAN ? v != v : false));
-      if (valid && isfinite(v)) mu = v;
-    }
-    unsigned long long* nanrow = reinterpret_cast<unsigned long long*>(sm + L.nanrow) + tb * g.R;
-    uint8_t* ctr = sm + L.ctr + tb * (kM * kTN);
-    for (int i = tid; i < g.R; i += kThreadsTC) nanrow[i] = 0ull;
-    __syncthreads();
-
-    const uint32_t abuf = b * L.a_stride;
-    bool any_invalid = false, any_nan = false;
-    const int items = g.KC * g.R;
-    for (int itm = tid; itm < items; itm += kThreadsTC) {
-      const int kc = itm / g.R, rho = itm - kc * g.R;
-      const int64_t yy = gy0 + rho;
-      const bool row_in = yy >= 0 && yy < a.H;
-      float hi[8], lo[8], vd[8];
-      unsigned long long nanbits = 0ull;
-#pragma unroll
-      for (int e = 0; e < 8; ++e) {
-        const int kp = g.Kp - 1 - (8 * kc + e);
-        float z = 0.0f, valid = 0.0f;
-        if (kp < g.KW) {
-          const int64_t xx = gx0 + kp;
-          const float v = stage[rho * g.BW + off + kp];
-          const bool inb = row_in && xx >= 0 && xx < a.W;
-          const bool okv = inb && !(a.nd.kind == VSR_NODATA_VALUE ? v == a.nd.fv
-                                                                  : (a.nd.kind == VSR_NODATA_NAN ? v != v : false));
-          // reference product v * w * valid: NaN (and inf * 0) poison the window
-          if (inb && !isfinite(v * (okv ? 1.0f : 0.0f))) nanbits |= 1ull << kp;
-          if (okv && isfinite(v)) {
-            z = v - mu;
-            valid = 1.0f;
+  if (warp == 0) {
+    // ========================================================= MMA issuer
+    if (lane == 0) {
+      const uint32_t lbo_a = static_cast<uint32_t>(g.Rp) * 16;
+      const uint32_t a_ks = (2 * lbo_a) >> 4;  // one k-step = two core matrices along K
+      uint32_t u = 0;                          // band-ring uses
+      int j = 0;
+      bool ok = true;
+      for (int64_t t = blockIdx.x; t < total; t += gridDim.x, ++j) {
+        const int b = j % a.nbuf, tb = j % L.tbuf, slot = j & 1;
+        ok = wait_or_abort(&a_full[b], (j / a.nbuf) & 1, &abort_flag, err_word, kDevErrMmaTimeout);
+        if (ok && j >= L.tbuf)
+          ok = wait_or_abort(&acc_empty[tb], ((j / L.tbuf) - 1) & 1, &abort_flag, err_word, kDevErrMmaTimeout);
+        if (!ok) break;
+        tc_fence_after();
+        const bool den_mma = info_nd[slot] != 0;
+        const uint32_t w_ahi = desc_lo(s_base + L.a_hi + b * L.a_bytes, lbo_a);
+        const uint32_t w_alo = desc_lo(s_base + L.a_lo + b * L.a_bytes, lbo_a);
+        const uint32_t w_avd = desc_lo(s_base + L.a_vd + b * L.a_bytes, lbo_a);
+        const uint32_t t_acc = tmem + tb * L.cols;
+        const uint32_t t_corr = t_acc + g.G * kTN, t_den = t_acc + (g.G + 1) * kTN;
+        for (int ky = 0; ky < a.kh; ++ky, ++u) {
+          const uint32_t s = u % kStages;
+          ok = wait_or_abort(&b_full[s], (u / kStages) & 1, &abort_flag, err_word, kDevErrMmaTimeout);
+          if (!ok) break;
+          tc_fence_after();
+          const int grp = (ky * g.G) / a.kh;
+          const uint32_t f = (ky == 0 || ((ky - 1) * g.G) / a.kh != grp) ? 0u : 1u;  // first row of its group
+          const uint32_t tg = t_acc + grp * kTN, td = t_den + grp * kTN;
+          // A_ky = the window advanced ky rows (16 bytes each); one k-step =
+          // two core matrices along K on both operands
+          uint32_t ah = w_ahi + ky, al = w_alo + ky, av = w_avd + ky;
+          uint32_t bh = desc_lo(s_base + L.ring + s * L.stage_bytes, 128), bl = bh + g.NB * 8;
+          mma_bf16(tg, ah, bh, f);
+          mma_bf16(t_corr, ah, bl, ky != 0);
+          mma_bf16(t_corr, al, bh, 1u);
+          if (den_mma) {
+            mma_bf16(td, av, bh, f);
+            mma_bf16(td, av, bl, 1u);
+#pragma unroll 1
+            for (int ks = 1; ks < g.KS; ++ks) {
+              ah += a_ks;
+              al += a_ks;
+              av += a_ks;
+              bh += 16;
+              bl += 16;
+              mma_bf16(tg, ah, bh, 1u);
+              mma_bf16(t_corr, ah, bl, 1u);
+              mma_bf16(t_corr, al, bh, 1u);
+              mma_bf16(td, av, bh, 1u);
+              mma_bf16(td, av, bl, 1u);
+            }
+          } else {
+#pragma unroll 2
+            for (int ks = 1; ks < g.KS; ++ks) {
+              ah += a_ks;
+              al += a_ks;
+              bh += 16;
+              bl += 16;
+              mma_bf16(tg, ah, bh, 1u);
+              mma_bf16(t_corr, ah, bl, 1u);
+              mma_bf16(t_corr, al, bh, 1u);
+            }
           }
-          any_invalid |= !okv;
-          const int m = rho - a.kh / 2, n = kp - a.kw / 2;
-          if (m >= 0 && m < kM && n >= 0 && n < kTN) ctr[m * kTN + n] = okv ? 1 : 0;
+          mma_commit(&b_empty[s]);  // the band stage is free once these MMAs have read it
         }
-        const float h = __bfloat162float(__float2bfloat16_rn(z));
-        hi[e] = h;
-        lo[e] = z - h;
-        vd[e] = valid;
+        if (!ok) break;
+        mma_commit(&a_empty[b]);
+        mma_commit(&acc_full[tb]);
       }
-      if (nanbits) {
-        any_nan = true;
-        atomicOr(&nanrow[rho], nanbits);
+      if (!ok) {
+        // MMAs already issued must finish before tensor memory is released
+        mma_commit(&drain_bar);
+        mbar_wait_bounded(&drain_bar, 0, err_word, kDevErrMmaTimeout);
       }
-      const uint32_t o = abuf + static_cast<uint32_t>(kc) * g.R * 16 + rho * 16;
-      *reinterpret_cast<uint4*>(sm + L.a_hi + o) =
-          make_uint4(pack_bf16x2(hi[0], hi[1]), pack_bf16x2(hi[2], hi[3]), pack_bf16x2(hi[4], hi[5]), pack_bf16x2(hi[6], hi[7]));
-      *reinterpret_cast<uint4*>(sm + L.a_lo + o) =
-          make_uint4(pack_bf16x2(lo[0], lo[1]), pack_bf16x2(lo[2], lo[3]), pack_bf16x2(lo[4], lo[5]), pack_bf16x2(lo[6], lo[7]));
-      *reinterpret_cast<uint4*>(sm + L.a_valid + o) =
-          make_uint4(pack_bf16x2(vd[0], vd[1]), pack_bf16x2(vd[2], vd[3]), pack_bf16x2(vd[4], vd[5]), pack_bf16x2(vd[6], vd[7]));
     }
-    fence_proxy_async_smem();
-    const bool has_invalid = __syncthreads_or(any_invalid);
-    const bool has_nan = __syncthreads_or(any_nan);
-    if (tid == 0) {
-      info_x0[tb] = x0;
-      info_y0[tb] = y0;
-      info_mu[tb] = mu;
-      info_inv[tb] = has_invalid;
-      info_nan[tb] = has_nan;
-      // the staging buffer is consumed: prefetch the next tile's window
-      const int64_t nt = t + gridDim.x;
-      if (nt < total) issue(nt);
-      tc_fence_after();
-      // descriptors advance by plain adds on the 16-byte start-address field
-      const uint64_t d_ahi = smem_desc(s_base + L.a_hi + abuf, lbo_a, 128);
-      const uint64_t d_alo = smem_desc(s_base + L.a_lo + abuf, lbo_a, 128);
-      const uint64_t d_av = smem_desc(s_base + L.a_valid + abuf, lbo_a, 128);
-      const uint64_t d_b = smem_desc(s_base + L.bw, 128, 128);
-      const uint64_t a_ks = 2 * lbo_a >> 4, b_band = static_cast<uint64_t>(g.NB) * 8;
-      const uint32_t t_acc = tmem + tb * cols_per_buf;
-      const uint32_t t_corr = t_acc + 64, t_den = t_acc + 96;
-      for (int ky = 0; ky < a.kh; ++ky) {
-        const int grp = (ky * G) / a.kh;
-        const bool grp_first = ky == 0 || ((ky - 1) * G) / a.kh != grp;
-        const uint64_t bh0 = d_b + static_cast<uint64_t>(2 * ky) * b_band;
-        const uint64_t bl0 = bh0 + b_band;
-        for (int ks = 0; ks < g.KS; ++ks) {
-          const uint64_t ao = static_cast<uint64_t>(ky) + ks * a_ks;
-          const uint64_t bo = static_cast<uint64_t>(ks) * 16;  // 2 core matrices of 128 B
-          mma_bf16(t_acc + grp * kTN, d_ahi + ao, bh0 + bo, !(grp_first && ks == 0));
-          mma_bf16(t_corr, d_ahi + ao, bl0 + bo, (ky | ks) != 0);
-          mma_bf16(t_corr, d_alo + ao, bh0 + bo, 1);
-          if (has_invalid) {
-            mma_bf16(t_den + grp * kTN, d_av + ao, bh0 + bo, !(grp_first && ks == 0));
-            mma_bf16(t_den + grp * kTN, d_av + ao, bl0 + bo, 1);
+  } else if (warp == 1) {
+    // ========================================================= band producer
+    if (lane == 0) {
+      uint32_t u = 0;
+      bool ok = true;
+      for (int64_t t = blockIdx.x; t < total && ok; t += gridDim.x) {
+        for (int ky = 0; ky < a.kh; ++ky, ++u) {
+          const uint32_t s = u % kStages;
+          if (u >= kStages) {
+            ok = wait_or_abort(&b_empty[s], ((u / kStages) - 1) & 1, &abort_flag, err_word, kDevErrTmaTimeout);
+            if (!ok) break;
           }
+          mbar_arrive_expect_tx(&b_full[s], L.stage_bytes);
+          bulk_g2s(sm + L.ring + s * L.stage_bytes, a.bw_img + static_cast<size_t>(ky) * L.stage_bytes,
+                   L.stage_bytes, &b_full[s]);
         }
       }
-      mma_commit(&mma_bar[tb]);
-    }
-    // horizontal NaN footprint of this tile (read by its epilogue later)
-    if (has_nan) {
-      for (int rho = tid; rho < g.R; rho += kThreadsTC) {
-        const unsigned long long mrow = nanrow[rho];
-        unsigned long long h = 0ull;
-        for (int j = 0; j < a.kw; ++j) h |= mrow >> j;  // bit n: a NaN in columns [n, n+kw)
-        nanrow[rho] = h;
+      if (!ok) {
+        // every stage's newest copy must land before shared memory is released
+        for (uint32_t k = (u > kStages ? u - kStages : 0u); k < u; ++k)
+          mbar_wait_bounded(&b_full[k % kStages], (k / kStages) & 1, err_word, kDevErrTmaTimeout);
       }
     }
-    // epilogue of the previous tile while the tensor core works on this one
-    if (prev_pending) {
-      if (a.nbuf == 2) {
-        const bool done = mbar_wait_bounded(&mma_bar[tb ^ 1], mma_phase[tb ^ 1], err_word, kDevErrMmaTimeout);
-        if (__syncthreads_or(!done)) { failed = true; break; }
+  } else {
+    // ========================================================= converters + epilogue
+    const int cw = warp - 2;            // converter warp 0..7
+    const int ct = tid - 64;            // converter thread
+    const int quarter = warp & 3;       // the TMEM lane quarter this warp may read
+    const int chalf = cw >> 2;          // epilogue: output columns 32*chalf .. +31
+    const int m = quarter * 32 + lane;  // epilogue: output row in the tile
+    const int kh2 = a.kh / 2, kw2 = a.kw / 2;
+    const int S1 = a.kw + 1;
+    const float wtot = static_cast<float>(sat[a.kh * S1 + a.kw]);
+    const float inv_wtot = __frcp_rn(wtot);
+    // this lane's window columns 4*lane .. 4*lane+3; in the K-reversed A
+    // layout they are elements klo+3 .. klo of one core-matrix row, so each
+    // operand takes one 8-byte store per window row
+    const int kp0 = 4 * lane;
+    const bool lane_cols = kp0 < g.KW;
+    const int klo = g.Kp - 4 - kp0;
+    const uint32_t o_lane = lane_cols ? static_cast<uint32_t>(klo >> 3) * g.Rp * 16 + (klo & 7) * 2 : 0u;
+    bool ok = true;
+
+    auto epilogue = [&](int jj) {
+      const int tb = jj % L.tbuf, slot = jj & 1;
+      const bool got = wait_or_abort(&acc_full[tb], (jj / L.tbuf) & 1, &abort_flag, err_word, kDevErrMmaTimeout);
+      if (conv_any(!got)) {
+        ok = false;
+        return;
       }
-      mma_phase[tb ^ 1] ^= 1;
       tc_fence_after();
-      epilogue(tb ^ 1);
+      const int64_t x0 = info_x0[slot], y0 = info_y0[slot];
+      const float mu = info_mu[slot];
+      const bool den_mma = info_nd[slot] != 0;
+      const int64_t y = y0 + m;
+      // centre validity of this row's 64 outputs
+      uint64_t cbits;
+      if (ND == 0) {
+        const int64_t nx = a.W - x0;
+        cbits = y >= a.H ? 0ull : (nx >= 64 ? ~0ull : ((1ull << nx) - 1ull));
+      } else {
+        const unsigned __int128 okm = reinterpret_cast<const unsigned __int128*>(sm + L.okrow)[slot * g.R + m + kh2];
+        cbits = static_cast<uint64_t>(okm >> kw2);
+      }
+      unsigned __int128 foot = 0, ifoot = 0;
+      if (info_nan[slot]) {
+        const unsigned __int128* nr = reinterpret_cast<const unsigned __int128*>(sm + L.nanrow) + slot * g.R;
+        for (int r2 = 0; r2 < a.kh; ++r2) foot |= nr[m + r2];
+      }
+      if (info_inf[slot]) {
+        const unsigned __int128* ir = reinterpret_cast<const unsigned __int128*>(sm + L.infrow) + slot * g.R;
+        for (int r2 = 0; r2 < a.kh; ++r2) ifoot |= ir[m + r2];
+      }
+      const uint32_t lane_base = tmem + tb * L.cols + (static_cast<uint32_t>(quarter * 32) << 16);
+      // the output row's window rows clipped to the raster (summed-area table rows);
+      // float64: a clipped window's sum is a difference of larger prefix sums
+      const int ky_lo = static_cast<int>(clamp64(kh2 - y, 0, a.kh));
+      const int ky_hi = static_cast<int>(clamp64(a.H - y + kh2, ky_lo, a.kh));
+      const double* s_lo = sat + ky_lo * S1;
+      const double* s_hi = sat + ky_hi * S1;
+      const bool interior = ky_lo == 0 && ky_hi == a.kh && x0 - kw2 >= 0 && x0 + kTN - 1 + (a.kw - 1 - kw2) < a.W;
+#pragma unroll 1
+      for (int sc = 0; sc < 2; ++sc) {
+        const int c0 = chalf * 32 + sc * 16;  // first of this pass's 16 output columns
+        float num[16], den[16], part[16];
+        tmem_ld16(lane_base + c0, num);
+        for (int gi = 1; gi < g.G; ++gi) {
+          tmem_ld16(lane_base + gi * kTN + c0, part);
+#pragma unroll
+          for (int n = 0; n < 16; ++n) num[n] += part[n];
+        }
+        tmem_ld16(lane_base + g.G * kTN + c0, part);  // correction products
+#pragma unroll
+        for (int n = 0; n < 16; ++n) num[n] += part[n];
+        if (ND != 0 && den_mma) {
+          tmem_ld16(lane_base + (g.G + 1) * kTN + c0, den);
+          for (int gi = 1; gi < g.G; ++gi) {
+            tmem_ld16(lane_base + (g.G + 1 + gi) * kTN + c0, part);
+#pragma unroll
+            for (int n = 0; n < 16; ++n) den[n] += part[n];
+          }
+        } else if (interior) {
+#pragma unroll
+          for (int n = 0; n < 16; ++n) den[n] = wtot;
+        } else {
+#pragma unroll
+          for (int n = 0; n < 16; ++n) {
+            const int64_t x = x0 + c0 + n;
+            const int kx_lo = static_cast<int>(clamp64(kw2 - x, 0, a.kw));
+            const int kx_hi = static_cast<int>(clamp64(a.W - x + kw2, kx_lo, a.kw));
+            den[n] = static_cast<float>((s_hi[kx_hi] - s_lo[kx_hi]) - (s_hi[kx_lo] - s_lo[kx_lo]));
+          }
+        }
+        if (y < a.H) {
+          const int64_t xb = x0 + c0;
+          const uint32_t cb = static_cast<uint32_t>(cbits >> c0) & 0xFFFFu;
+          const uint32_t fb = static_cast<uint32_t>(static_cast<uint64_t>(foot >> c0)) & 0xFFFFu;
+          const uint32_t ib = static_cast<uint32_t>(static_cast<uint64_t>(ifoot >> c0)) & 0xFFFFu & ~fb;
+          uint32_t ndm = 0;  // outputs that take the nodata value
+#pragma unroll
+          for (int n = 0; n < 16; ++n) {
+            const bool nd = !((cb >> n) & 1u) || !(den[n] > 0.0f);
+            ndm |= static_cast<uint32_t>(nd) << n;
+            const float inv = (ND == 0 || !den_mma) && interior ? inv_wtot : __frcp_rn(den[n]);
+            num[n] = ((fb >> n) & 1u) ? __int_as_float(0x7fc00000) : fmaf(num[n], inv, mu);
+          }
+          for (uint32_t r = ib & ~ndm; r; r &= r - 1) {  // windows holding +-inf (rare)
+            const int n = __ffs(r) - 1;
+            if (xb + n < a.W) {
+              const float v = inf_window(a.src, a.H, a.W, a.pitch, a.w64, a.kh, a.kw, a.nd_kind, a.nd_f, y, xb + n);
+#pragma unroll
+              for (int q = 0; q < 16; ++q)
+                if (q == n) num[q] = v;
+            }
+          }
+          if (a.out_dtype == VSR_F64) {
+            double* row = static_cast<double*>(a.dst) + y * a.out_pitch + xb;
+#pragma unroll
+            for (int n = 0; n < 16; ++n)
+              if (xb + n < a.W) row[n] = ((ndm >> n) & 1u) ? a.nd_out : static_cast<double>(num[n]);
+          } else {
+            const float ndf = static_cast<float>(a.nd_out);
+#pragma unroll
+            for (int n = 0; n < 16; ++n) num[n] = ((ndm >> n) & 1u) ? ndf : num[n];
+            float* row = static_cast<float*>(a.dst) + y * a.out_pitch + xb;
+            if (a.vec_out && xb + 16 <= a.W) {
+#pragma unroll
+              for (int q = 0; q < 4; ++q)
+                reinterpret_cast<float4*>(row)[q] = make_float4(num[4 * q], num[4 * q + 1], num[4 * q + 2], num[4 * q + 3]);
+            } else {
+#pragma unroll
+              for (int n = 0; n < 16; ++n)
+                if (xb + n < a.W) row[n] = num[n];
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(&acc_empty[tb]);
+    };
+
+    int j = 0;
+    for (int64_t t = blockIdx.x; t < total; t += gridDim.x, ++j) {
+      const int b = j % a.nbuf, slot = j & 1;
+      if (j >= a.nbuf) {
+        const bool got = wait_or_abort(&a_empty[b], ((j / a.nbuf) - 1) & 1, &abort_flag, err_word, kDevErrMmaTimeout);
+        if (conv_any(!got)) {
+          ok = false;
+          break;
+        }
+      }
+      const int64_t ty = t / tiles_x;
+      const int64_t x0 = (t - ty * tiles_x) * kTN, y0 = ty * kM;
+      const int64_t gx0 = x0 - kw2, gy0 = y0 - kh2;
+      float mu = 0.0f;
+      {
+        // the window's centre pixel, moved inside the raster on edge tiles
+        // (a centre far from the tile's values would cost accumulator bits)
+        const int64_t yy = clamp64(gy0 + g.R / 2, 0, a.H - 1), xx = clamp64(gx0 + g.KW / 2, 0, a.W - 1);
+        const float v = __ldg(a.src + yy * a.pitch + xx);
+        const bool nd = ND == 1 ? v == a.nd_f : (ND == 2 ? v != v : false);
+        if (!nd && isfinite(v)) mu = v;
+      }
+      uint32_t colv = 0;  // this lane's columns inside the window and the raster
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int64_t xx = gx0 + kp0 + q;
+        colv |= static_cast<uint32_t>(kp0 + q < g.KW && xx >= 0 && xx < a.W) << q;
+      }
+      uint32_t* nanw = reinterpret_cast<uint32_t*>(sm + L.nanrow) + slot * g.R * 4;
+      uint32_t* infw = reinterpret_cast<uint32_t*>(sm + L.infrow) + slot * g.R * 4;
+      uint32_t* okw = reinterpret_cast<uint32_t*>(sm + L.okrow) + slot * g.R * 4;
+      unsigned char* ahi = sm + L.a_hi + b * L.a_bytes + o_lane;
+      unsigned char* alo = sm + L.a_lo + b * L.a_bytes + o_lane;
+      unsigned char* avd = sm + L.a_vd + b * L.a_bytes + o_lane;
+      bool any_nan = false, any_inf = false, any_nd = false;
+      // one warp per window row, 4 columns per lane; kConvRows rows are
+      // loaded before any is converted, so the loads' latencies overlap
+      for (int r0 = cw; r0 < g.R; r0 += kConvWarps * kConvRows) {
+        float vb[kConvRows][4];
+#pragma unroll
+        for (int r = 0; r < kConvRows; ++r) {
+          const int rho = r0 + kConvWarps * r;
+          const int64_t yy = gy0 + rho;
+          const uint32_t in = (rho < g.R && yy >= 0 && yy < a.H) ? colv : 0u;
+          const int64_t base = (in ? yy : 0) * a.pitch + gx0 + kp0;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) vb[r][q] = ((in >> q) & 1u) ? __ldg(a.src + base + q) : 0.0f;
+        }
+#pragma unroll
+        for (int r = 0; r < kConvRows; ++r) {
+          const int rho = r0 + kConvWarps * r;
+          if (rho >= g.R) break;
+          const int64_t yy = gy0 + rho;
+          const uint32_t in = (yy >= 0 && yy < a.H) ? colv : 0u;
+          float z[4];
+          uint32_t okm = 0, badm = 0;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const float v = vb[r][q];
+            const bool inb = (in >> q) & 1u;
+            const bool okv = inb && (ND == 1 ? v != a.nd_f : (ND == 2 ? v == v : true));
+            const bool fin = fabsf(v) <= 3.402823466e38f;  // false for NaN and +-inf
+            z[q] = (okv && fin) ? v - mu : 0.0f;
+            okm |= static_cast<uint32_t>(okv) << q;
+            badm |= static_cast<uint32_t>(inb && !fin) << q;
+          }
+          if (ND != 0) any_nd |= okm != in;
+          if (lane_cols) {
+            const __nv_bfloat162 h32 = __floats2bfloat162_rn(z[3], z[2]);
+            const __nv_bfloat162 h10 = __floats2bfloat162_rn(z[1], z[0]);
+            const __nv_bfloat162 l32 = __floats2bfloat162_rn(z[3] - __low2float(h32), z[2] - __high2float(h32));
+            const __nv_bfloat162 l10 = __floats2bfloat162_rn(z[1] - __low2float(h10), z[0] - __high2float(h10));
+            *reinterpret_cast<uint2*>(ahi + rho * 16) = make_uint2(bf16x2_bits(h32), bf16x2_bits(h10));
+            *reinterpret_cast<uint2*>(alo + rho * 16) = make_uint2(bf16x2_bits(l32), bf16x2_bits(l10));
+            if (ND != 0)
+              *reinterpret_cast<uint2*>(avd + rho * 16) =
+                  make_uint2(((okm & 8u) ? 0x3f80u : 0u) | ((okm & 4u) ? 0x3f800000u : 0u),
+                             ((okm & 2u) ? 0x3f80u : 0u) | ((okm & 1u) ? 0x3f800000u : 0u));
+          }
+          uint32_t bq[4];
+          if (__any_sync(0xffffffffu, badm != 0)) {
+            // NaN taps poison the window (reference product v * w * valid,
+            // NaN * 0 included); valid +-inf taps make it infinite (inf_window)
+            uint32_t pm = 0, im = 0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              const float v = vb[r][q];
+              const float vm = v * (((okm >> q) & 1u) ? 1.0f : 0.0f);
+              pm |= static_cast<uint32_t>(((in >> q) & 1u) && vm != vm) << q;
+              im |= static_cast<uint32_t>(((okm >> q) & 1u) && isinf(v)) << q;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) bq[q] = __ballot_sync(0xffffffffu, (pm >> q) & 1u);
+            const uint32_t wn = interleave4(bq, lane & 3);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) bq[q] = __ballot_sync(0xffffffffu, (im >> q) & 1u);
+            const uint32_t wi = interleave4(bq, lane & 3);
+            if (lane < 4) {
+              nanw[rho * 4 + lane] = wn;
+              infw[rho * 4 + lane] = wi;
+            }
+            any_nan |= pm != 0;
+            any_inf |= im != 0;
+          } else if (lane < 4) {
+            nanw[rho * 4 + lane] = 0u;
+            infw[rho * 4 + lane] = 0u;
+          }
+          if (ND != 0) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) bq[q] = __ballot_sync(0xffffffffu, (okm >> q) & 1u);
+            const uint32_t wo = interleave4(bq, lane & 3);
+            if (lane < 4) okw[rho * 4 + lane] = wo;
+          }
+        }
+      }
+      fence_proxy_async_smem();  // generic-proxy operand writes -> visible to the tensor core
+      const bool tile_nan = conv_any(any_nan);
+      const bool tile_inf = conv_any(any_inf);
+      const bool tile_nd = ND != 0 && conv_any(any_nd);
+      if (ct == 0) {
+        info_x0[slot] = x0;
+        info_y0[slot] = y0;
+        info_mu[slot] = mu;
+        info_nan[slot] = tile_nan;
+        info_inf[slot] = tile_inf;
+        info_nd[slot] = tile_nd;
+      }
+      mbar_arrive(&a_full[b]);
+      // horizontal footprints (bit n: such a tap in window columns [n, n+kw))
+      if (tile_nan || tile_inf) {
+        unsigned __int128* nanrow = reinterpret_cast<unsigned __int128*>(sm + L.nanrow) + slot * g.R;
+        unsigned __int128* infrow = reinterpret_cast<unsigned __int128*>(sm + L.infrow) + slot * g.R;
+        for (int rho = ct; rho < g.R; rho += kConvThreads) {
+          const unsigned __int128 mrow = nanrow[rho], irow = infrow[rho];
+          unsigned __int128 h = 0, hi = 0;
+          for (int q = 0; q < a.kw; ++q) {
+            h |= mrow >> q;
+            hi |= irow >> q;
+          }
+          nanrow[rho] = h;
+          infrow[rho] = hi;
+        }
+      }
+      if (j >= 1) {
+        epilogue(j - 1);
+        if (!ok) break;
+      }
+      conv_sync();  // this iteration's reads of the older slot end before the next tile rewrites it
     }
-    prev_pending = true;
-    tc_fence_before();
-    __syncthreads();
+    if (ok && j >= 1) epilogue(j - 1);
   }
-  if (!failed && prev_pending) {
-    const int tb = (it - 1) & 1;
-    const bool done = mbar_wait_bounded(&mma_bar[tb], mma_phase[tb], err_word, kDevErrMmaTimeout);
-    if (!__syncthreads_or(!done)) {
-      tc_fence_after();
-      epilogue(tb);
-    } else {
-      failed = true;
-    }
-  }
-  if (failed && tid == 0) {
-    // A copy may still be in flight into the staging buffer: give it a
-    // bounded chance to land before shared memory is released.
-    mbar_wait_bounded(&tma_bar, tma_phase, err_word, kDevErrTmaTimeout);
-  }
+  __syncwarp();
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {
+    __syncwarp();
     tc_fence_after();
     tmem_dealloc(tmem, 512);
   }
 }
 
-// Toeplitz band images: for ky, split s in {hi, lo}, core matrix c, row r,
-// element e -> w[ky][Kp-1-8c-e-r] (0 outside [0, kw)), split as
-// w = bf16(w) + bf16(w - bf16(w)); also the total of (w_hi + w_lo).
+// Toeplitz band images: for kernel row ky, split s in {hi, lo}, core matrix
+// c, row r, element e -> w[ky][Kp-1-8c-e-r] (0 outside [0, kw)), split as
+// w = bf16(w) + bf16(w - bf16(w)); laid out [ky][s][c][r][e] so a kernel
+// row's two bands are one contiguous copy.
 __global__ void prep_tc_weights(const double* __restrict__ w64, int kh, int kw, int Kp, int NB,
-                                uint16_t* __restrict__ img, float* __restrict__ wsum) {
+                                uint16_t* __restrict__ img) {
   const int per_row = NB * 64;
   const int total = kh * per_row;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
@@ -487,37 +769,45 @@ __global__ void prep_tc_weights(const double* __restrict__ w64, int kh, int kw, 
     img[((ky * 2 + 0) * NB + c) * 64 + r * 8 + e] = __bfloat16_as_ushort(hi);
     img[((ky * 2 + 1) * NB + c) * 64 + r * 8 + e] = __bfloat16_as_ushort(lo);
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    double s = 0.0;
-    for (int i = 0; i < kh * kw; ++i) {
-      const __nv_bfloat16 hi = __float2bfloat16_rn(static_cast<float>(w64[i]));
-      const double h = __bfloat162float(hi);
-      const double l = __bfloat162float(__float2bfloat16_rn(static_cast<float>(w64[i] - h)));
-      s += h + l;
+}
+
+// Summed-area table of the split weights w_hi + w_lo in float64:
+// sat[i][j] = sum of w over rows < i and columns < j.  One thread per column j.
+__global__ void prep_tc_sat(const double* __restrict__ w64, int kh, int kw, double* __restrict__ sat) {
+  const int j = threadIdx.x;
+  if (blockIdx.x != 0 || j > kw) return;
+  double acc = 0.0;
+  sat[j] = 0.0;
+  for (int i = 1; i <= kh; ++i) {
+    for (int c = 0; c < j; ++c) {
+      const double w = w64[(i - 1) * kw + c];
+      const double h = __bfloat162float(__float2bfloat16_rn(static_cast<float>(w)));
+      acc += h + static_cast<double>(__bfloat162float(__float2bfloat16_rn(static_cast<float>(w - h))));
     }
-    wsum[0] = static_cast<float>(s);
+    sat[i * (kw + 1) + j] = acc;
   }
 }
 
 }  // namespace
 
-static int tc_nbuf(int kh, int kw) {
+static int tc_nbuf(int kh, int kw, bool has_nd) {
   const TcGeom g = make_geom(kh, kw);
-  return make_smem(g, 2).total + 1024 <= 227 * 1024 ? 2 : 1;
+  return make_plan(g, has_nd, 2).total + 1024 <= 227 * 1024 ? 2 : 1;
 }
 
 int conv_tc_supported(int kh, int kw) {
   if (kh < 1 || kw < 1 || kh > kMaxTCK || kw > kMaxTCK) return 0;
   const TcGeom g = make_geom(kh, kw);
-  return make_smem(g, 1).total + 1024 <= 227 * 1024 && g.KW <= 64 && g.BW <= 256 && g.R <= 256;
+  return make_plan(g, true, 1).total + 1024 <= 227 * 1024 && g.KW <= 128 && make_plan(g, true, 1).cols <= 512;
 }
 
-// Workspace: float64 weights | Toeplitz images | total.
+// Workspace: float64 weights | Toeplitz band images | summed-area table.
 size_t conv_tc_workspace(int kh, int kw) {
   const TcGeom g = make_geom(kh, kw);
   const size_t a = (static_cast<size_t>(kh) * kw * 8 + 255) & ~size_t(255);
   const size_t b = (static_cast<size_t>(kh) * 2 * g.NB * 128 + 255) & ~size_t(255);
-  return a + b + 256;
+  const size_t c = (static_cast<size_t>(kh + 1) * (kw + 1) * 8 + 255) & ~size_t(255);
+  return a + b + c;
 }
 
 int run_conv_tc(const void* src, int dtype, int64_t H, int64_t W, int64_t pitch, const double* weights_host, int kh,
@@ -526,38 +816,38 @@ int run_conv_tc(const void* src, int dtype, int64_t H, int64_t W, int64_t pitch,
   if (dtype != VSR_F32) return fail(VSR_ERR_UNSUPPORTED, "split-BF16 convolution reads float32 rasters");
   if (!conv_tc_supported(kh, kw))
     return fail(VSR_ERR_UNSUPPORTED, "split-BF16 convolution supports kernels up to %dx%d", kMaxTCK, kMaxTCK);
-  if (!aligned(src, 16) || (pitch % 4) != 0)
-    return fail(VSR_ERR_UNSUPPORTED, "split-BF16 convolution needs 16-byte aligned rows");
   const size_t need = conv_tc_workspace(kh, kw);
   if (!workspace || ws_bytes < need || !aligned(workspace, 256))
     return fail(VSR_ERR_WORKSPACE, "workspace must be 256-byte aligned and >= %zu bytes", need);
   const TcGeom g = make_geom(kh, kw);
-  const int nbuf = tc_nbuf(kh, kw);
-  const TcSmem L = make_smem(g, nbuf);
+  double ndv = 0.0;
+  const int kind = resolve_nodata(VSR_F32, nodata, nodata_kind, &ndv);
+  const bool has_nd = kind != VSR_NODATA_NONE;
+  const int nbuf = tc_nbuf(kh, kw, has_nd);
+  const TcPlan L = make_plan(g, has_nd, nbuf);
   char* ws = static_cast<char*>(workspace);
   double* w64 = reinterpret_cast<double*>(ws);
   const size_t off_img = (static_cast<size_t>(kh) * kw * 8 + 255) & ~size_t(255);
+  const size_t off_sat = off_img + ((static_cast<size_t>(kh) * 2 * g.NB * 128 + 255) & ~size_t(255));
   uint16_t* img = reinterpret_cast<uint16_t*>(ws + off_img);
-  float* wsum = reinterpret_cast<float*>(ws + need - 256);
+  double* sat = reinterpret_cast<double*>(ws + off_sat);
   VSR_CUDA_TRY(cudaMemcpyAsync(w64, weights_host, static_cast<size_t>(kh) * kw * 8, cudaMemcpyHostToDevice, st));
-  prep_tc_weights<<<16, 256, 0, st>>>(w64, kh, kw, g.Kp, g.NB, img, wsum);
+  prep_tc_weights<<<16, 256, 0, st>>>(w64, kh, kw, g.Kp, g.NB, img);
   VSR_CUDA_TRY(cudaGetLastError());
-
-  CUtensorMap map;
-  int rc = encode_tensor_map_2d(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, src, W, H, pitch, g.BW, g.R);
-  if (rc) return rc;
+  prep_tc_sat<<<1, 64, 0, st>>>(w64, kh, kw, sat);
+  VSR_CUDA_TRY(cudaGetLastError());
   uint32_t* err = device_error_word();
   if (!err) return VSR_ERR_CUDA;
-  double ndv = 0.0;
-  const int kind = resolve_nodata(VSR_F32, nodata, nodata_kind, &ndv);
-  TcArgs a{H, W, {kind, static_cast<float>(ndv)}, nodata, dst, out_dtype, out_pitch,
-           reinterpret_cast<const uint4*>(img), wsum, kh, kw, nbuf};
-  // At least 116 KB of shared memory keeps one CTA per SM.
+  const bool vec_out = out_dtype == VSR_F32 && aligned(dst, 16) && out_pitch % 4 == 0;
+  TcArgs a{static_cast<const float*>(src), H, W, pitch, kind, static_cast<float>(ndv), nodata, dst, out_dtype,
+           out_pitch, vec_out ? 1 : 0, reinterpret_cast<const unsigned char*>(img), sat, w64, kh, kw, nbuf};
+  // At least 116 KB of shared memory keeps one CTA (and its 512 TMEM columns) per SM.
   const size_t smem = std::max<size_t>(L.total + 1024, 116 * 1024);
-  VSR_CUDA_TRY(cudaFuncSetAttribute(conv_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  auto kern = kind == VSR_NODATA_NONE ? conv_tc_kernel<0> : (kind == VSR_NODATA_VALUE ? conv_tc_kernel<1> : conv_tc_kernel<2>);
+  VSR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   const int64_t tiles = ((W + kTN - 1) / kTN) * ((H + kM - 1) / kM);
   const int64_t grid = std::min<int64_t>(tiles, sm_count());
-  conv_tc_kernel<<<static_cast<unsigned>(grid), kThreadsTC, smem, st>>>(map, a, err);
+  kern<<<static_cast<unsigned>(grid), kThreadsTC, smem, st>>>(a, err);
   VSR_CUDA_TRY(cudaGetLastError());
   return VSR_OK;
 }

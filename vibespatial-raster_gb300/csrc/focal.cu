@@ -19,6 +19,7 @@
 //   mean = sum / count formed in float64 (reference: Welford in float64,
 //   kernels/focal.py:672-769 / scipy generic_filter, algebra.py:3083-3101).
 #include <algorithm>
+#include <cmath>
 
 #include "vsr_internal.cuh"
 
@@ -973,13 +974,23 @@ extern "C" int vsr_convolve(const void* src, int dtype, int64_t height, int64_t 
   if (precision < VSR_PREC_AUTO || precision > VSR_PREC_SPLIT_BF16) return fail(VSR_ERR_INVALID_ARG, "bad precision %d", precision);
   if (kh > kMaxDirectK || kw > kMaxDirectK)
     return fail(VSR_ERR_UNSUPPORTED, "kernel %dx%d larger than the supported %dx%d", kh, kw, kMaxDirectK, kMaxDirectK);
-  // Tensor-core path: float32 rasters with 16-byte aligned rows, kernels that
-  // fit its shared-memory plan; AUTO takes it for k >= 15 on both axes.
-  const bool tc_ok = dtype == VSR_F32 && conv_tc_supported(kh, kw) && aligned(src, 16) && pitch % 4 == 0;
+  // Tensor-core path: float32 rasters and kernels that fit its shared-memory
+  // plan.  AUTO takes it for k >= 15 on both axes when the kernel is well
+  // conditioned: split-BF16 weights carry 16 mantissa bits, and a weight sum
+  // that nearly cancels (sum |w| > 4 |sum w|) would amplify that rounding.
+  const bool tc_ok = dtype == VSR_F32 && conv_tc_supported(kh, kw) && aligned(src, 4);
   if (precision == VSR_PREC_SPLIT_BF16 && !tc_ok)
-    return fail(VSR_ERR_UNSUPPORTED,
-                "split-BF16 convolution needs a float32 raster with 16-byte aligned rows and a kernel of at most 41x41");
-  if (precision == VSR_PREC_SPLIT_BF16 || (precision == VSR_PREC_AUTO && tc_ok && kh >= 15 && kw >= 15))
+    return fail(VSR_ERR_UNSUPPORTED, "split-BF16 convolution needs a float32 raster and a kernel of at most 41x41");
+  bool well_conditioned = false;
+  if (precision == VSR_PREC_AUTO && tc_ok && kh >= 15 && kw >= 15) {
+    double s = 0.0, sa = 0.0;
+    for (int i = 0; i < kh * kw; ++i) {
+      s += weights_host[i];
+      sa += std::fabs(weights_host[i]);
+    }
+    well_conditioned = sa <= 4.0 * std::fabs(s);
+  }
+  if (precision == VSR_PREC_SPLIT_BF16 || well_conditioned)
     return run_conv_tc(src, dtype, height, width, pitch, weights_host, kh, kw, nodata, nodata_kind, dst, out_dtype,
                        out_pitch, workspace, workspace_bytes, static_cast<cudaStream_t>(stream));
   const size_t need = conv_ws_plain(kh, kw);

@@ -10,7 +10,7 @@
 // the output; its scratch (the staged float64 weights and the float32 or
 // BF16 operand images built from them) lives in a file-scope __device__ array sized
 // for the largest supported kernel of either precision.  Every GPU that
-// loads the library holds that array (kNoAllocScratchBytes, 105.75 KiB)
+// loads the library holds that array (kNoAllocScratchBytes, 242.5 KiB)
 // until the process exits.
 //
 // Host code cannot use the array's name as a device address, so on the first
@@ -34,9 +34,9 @@ constexpr int kNoAllocMaxK = 80;
 // The larger of the two workspaces vsr_convolve can ask for:
 //  * FP32 path, 80 x 80: 51,200 B float64 weights + 25,600 B float32 rows +
 //    256 B for the total = 77,056 B;
-//  * split-BF16 path, 41 x 41: 13,568 B float64 weights + 94,464 B Toeplitz
-//    images + 256 B = 108,288 B.
-constexpr size_t kNoAllocScratchBytes = 108288;
+//  * split-BF16 path, 41 x 41: 13,568 B float64 weights + 220,416 B Toeplitz
+//    band images + 14,336 B float64 summed-area table = 248,320 B.
+constexpr size_t kNoAllocScratchBytes = 248320;
 
 static __device__ __align__(256) unsigned char g_conv_scratch[kNoAllocScratchBytes];
 
