@@ -358,6 +358,11 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
     if (lane == 0) {
       const uint32_t lbo_a = static_cast<uint32_t>(g.Rp) * 16;
       const uint32_t a_ks = (2 * lbo_a) >> 4;  // one k-step = two core matrices along K
+      const uint32_t w_ring = desc_lo(s_base + L.ring, 128), stage_w = L.stage_bytes >> 4;
+      // first kernel rows of accumulator groups 1 and 2 (kh when absent):
+      // row ky belongs to group floor(ky G / kh)
+      const int gb1 = g.G > 1 ? (a.kh + g.G - 1) / g.G : a.kh;
+      const int gb2 = g.G > 2 ? (2 * a.kh + g.G - 1) / g.G : a.kh;
       uint32_t u = 0;                          // band-ring uses
       int j = 0;
       bool ok = true;
@@ -374,18 +379,21 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
         const uint32_t w_avd = desc_lo(s_base + L.a_vd + b * L.a_bytes, lbo_a);
         const uint32_t t_acc = tmem + tb * L.cols;
         const uint32_t t_corr = t_acc + g.G * kTN, t_den = t_acc + (g.G + 1) * kTN;
+        // Per kernel row: a few integer ops, then the MMAs (the thread's
+        // overhead between rows is time the tensor pipe may run dry).  The
+        // band-full wait needs no tcgen05 fence: the copy completes on the
+        // mbarrier itself.
         for (int ky = 0; ky < a.kh; ++ky, ++u) {
           const uint32_t s = u % kStages;
           ok = wait_or_abort(&b_full[s], (u / kStages) & 1, &abort_flag, err_word, kDevErrMmaTimeout);
           if (!ok) break;
-          tc_fence_after();
-          const int grp = (ky * g.G) / a.kh;
-          const uint32_t f = (ky == 0 || ((ky - 1) * g.G) / a.kh != grp) ? 0u : 1u;  // first row of its group
+          const int grp = (ky >= gb1) + (ky >= gb2);
+          const uint32_t f = (ky == 0 || ky == gb1 || ky == gb2) ? 0u : 1u;  // first row of its group
           const uint32_t tg = t_acc + grp * kTN, td = t_den + grp * kTN;
           // A_ky = the window advanced ky rows (16 bytes each); one k-step =
           // two core matrices along K on both operands
           uint32_t ah = w_ahi + ky, al = w_alo + ky, av = w_avd + ky;
-          uint32_t bh = desc_lo(s_base + L.ring + s * L.stage_bytes, 128), bl = bh + g.NB * 8;
+          uint32_t bh = w_ring + s * stage_w, bl = bh + g.NB * 8;
           mma_bf16(tg, ah, bh, f);
           mma_bf16(t_corr, ah, bl, ky != 0);
           mma_bf16(t_corr, al, bh, 1u);
@@ -772,19 +780,33 @@ __global__ void prep_tc_weights(const double* __restrict__ w64, int kh, int kw, 
 }
 
 // Summed-area table of the split weights w_hi + w_lo in float64:
-// sat[i][j] = sum of w over rows < i and columns < j.  One thread per column j.
+// sat[i][j] = sum of w over rows < i and columns < j.  One block: split
+// weights to shared memory, row prefix sums (a thread per row), then
+// column sums (a thread per column).
 __global__ void prep_tc_sat(const double* __restrict__ w64, int kh, int kw, double* __restrict__ sat) {
-  const int j = threadIdx.x;
-  if (blockIdx.x != 0 || j > kw) return;
-  double acc = 0.0;
-  sat[j] = 0.0;
-  for (int i = 1; i <= kh; ++i) {
-    for (int c = 0; c < j; ++c) {
-      const double w = w64[(i - 1) * kw + c];
-      const double h = __bfloat162float(__float2bfloat16_rn(static_cast<float>(w)));
-      acc += h + static_cast<double>(__bfloat162float(__float2bfloat16_rn(static_cast<float>(w - h))));
+  __shared__ double ws[kMaxTCK * kMaxTCK];
+  const int tid = threadIdx.x;
+  for (int i = tid; i < kh * kw; i += blockDim.x) {
+    const double w = w64[i];
+    const double h = __bfloat162float(__float2bfloat16_rn(static_cast<float>(w)));
+    ws[i] = h + static_cast<double>(__bfloat162float(__float2bfloat16_rn(static_cast<float>(w - h))));
+  }
+  __syncthreads();
+  if (tid < kh) {
+    double acc = 0.0;
+    for (int c = 0; c < kw; ++c) {
+      acc += ws[tid * kw + c];
+      ws[tid * kw + c] = acc;
     }
-    sat[i * (kw + 1) + j] = acc;
+  }
+  __syncthreads();
+  if (tid <= kw) {
+    double acc = 0.0;
+    sat[tid] = 0.0;
+    for (int i = 1; i <= kh; ++i) {
+      if (tid > 0) acc += ws[(i - 1) * kw + tid - 1];
+      sat[i * (kw + 1) + tid] = acc;
+    }
   }
 }
 
