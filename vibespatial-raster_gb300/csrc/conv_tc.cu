@@ -65,7 +65,8 @@ constexpr int kConvWarps = 8;      // warps 2..9
 constexpr int kConvThreads = 32 * kConvWarps;
 constexpr int kThreadsTC = 64 + kConvThreads;
 constexpr int kMaxTCK = 41;
-constexpr int kStages = 8;         // Toeplitz band ring depth
+constexpr int kMaxStages = 8;      // Toeplitz band ring depth (at most)
+constexpr int kRowsPerStage = 2;   // kernel rows per ring stage (one wait and one release per stage)
 constexpr int kConvRows = 6;       // window rows a converter warp loads per batch
 
 struct TcGeom {
@@ -101,7 +102,8 @@ __host__ __device__ inline TcGeom make_geom(int kh, int kw) {
 struct TcPlan {  // shared-memory byte offsets (1024-aligned base) and pipeline shape
   uint32_t a_bytes;             // one operand buffer
   uint32_t a_hi, a_lo, a_vd;    // nbuf buffers each
-  uint32_t ring, stage_bytes;   // kStages x (hi band, lo band)
+  uint32_t ring;                // nst stages of kRowsPerStage x (hi band, lo band)
+  uint32_t row_bytes, stage_bytes;
   uint32_t sat;                 // (kh+1) x (kw+1) doubles
   uint32_t ctr;                 // 2 x kM u64 centre-validity bits
   uint32_t nanrow;              // 2 x R unsigned __int128 NaN footprints
@@ -109,20 +111,23 @@ struct TcPlan {  // shared-memory byte offsets (1024-aligned base) and pipeline 
   uint32_t okrow;               // 2 x R unsigned __int128 validity masks (nodata rules)
   uint32_t total;
   int nbuf;                     // A buffers (1 or 2)
+  int nst;                      // ring stages
   int cols;                     // TMEM columns per accumulator buffer
   int tbuf;                     // TMEM accumulator buffers (1 or 2)
 };
 
-__host__ __device__ inline TcPlan make_plan(const TcGeom& g, bool has_nd, int nbuf) {
+__host__ __device__ inline TcPlan make_plan(const TcGeom& g, bool has_nd, int nbuf, int nst) {
   TcPlan p;
   p.nbuf = nbuf;
+  p.nst = nst;
   p.a_bytes = (static_cast<uint32_t>(g.KC) * g.Rp * 16 + 127) & ~127u;
   p.a_hi = 0;
   p.a_lo = p.a_hi + nbuf * p.a_bytes;
   p.a_vd = p.a_lo + nbuf * p.a_bytes;
   p.ring = p.a_vd + (has_nd ? nbuf * p.a_bytes : 0u);
-  p.stage_bytes = 2u * g.NB * 128;
-  p.sat = p.ring + kStages * p.stage_bytes;
+  p.row_bytes = 2u * g.NB * 128;
+  p.stage_bytes = kRowsPerStage * p.row_bytes;
+  p.sat = p.ring + nst * p.stage_bytes;
   p.ctr = (p.sat + static_cast<uint32_t>(g.kh + 1) * (g.kw + 1) * 8 + 127) & ~127u;
   p.nanrow = p.ctr + 2 * kM * 8;
   p.infrow = p.nanrow + 2 * static_cast<uint32_t>(g.R) * 16;
@@ -256,7 +261,7 @@ struct TcArgs {
   const double* sat;            // (kh+1) x (kw+1) prefix sums of w_hi + w_lo
   const double* w64;            // the kernel as given (windows holding +-inf)
   int kh, kw;
-  int nbuf;
+  int nbuf, nst;
 };
 
 __device__ __forceinline__ int64_t clamp64(int64_t v, int64_t lo, int64_t hi) {
@@ -310,8 +315,8 @@ __device__ __noinline__ float inf_window(const float* __restrict__ src, int64_t 
 template <int ND>
 __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, uint32_t* err_word) {
   extern __shared__ unsigned char tc_raw[];
-  __shared__ __align__(8) uint64_t a_full[2], a_empty[2], acc_full[2], acc_empty[2], b_full[kStages],
-      b_empty[kStages], drain_bar;
+  __shared__ __align__(8) uint64_t a_full[2], a_empty[2], acc_full[2], acc_empty[2], b_full[kMaxStages],
+      b_empty[kMaxStages], drain_bar;
   __shared__ uint32_t tmem_slot;
   __shared__ volatile int abort_flag;
   __shared__ int64_t info_x0[2], info_y0[2];
@@ -319,7 +324,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
   __shared__ int info_nan[2], info_inf[2], info_nd[2];
   unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tc_raw) + 1023) & ~uintptr_t(1023));
   const TcGeom g = make_geom(a.kh, a.kw);
-  const TcPlan L = make_plan(g, ND != 0, a.nbuf);
+  const TcPlan L = make_plan(g, ND != 0, a.nbuf, a.nst);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t tiles_x = (a.W + kTN - 1) / kTN;
   const int64_t total = tiles_x * ((a.H + kM - 1) / kM);
@@ -339,7 +344,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
       mbar_init(&acc_full[i], 1);
       mbar_init(&acc_empty[i], kConvThreads);
     }
-    for (int s = 0; s < kStages; ++s) {
+    for (int s = 0; s < L.nst; ++s) {
       mbar_init(&b_full[s], 1);
       mbar_init(&b_empty[s], 1);
     }
@@ -358,7 +363,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
     if (lane == 0) {
       const uint32_t lbo_a = static_cast<uint32_t>(g.Rp) * 16;
       const uint32_t a_ks = (2 * lbo_a) >> 4;  // one k-step = two core matrices along K
-      const uint32_t w_ring = desc_lo(s_base + L.ring, 128), stage_w = L.stage_bytes >> 4;
+      const uint32_t w_ring = desc_lo(s_base + L.ring, 128), stage_w = L.stage_bytes >> 4, row_w = L.row_bytes >> 4;
       // first kernel rows of accumulator groups 1 and 2 (kh when absent):
       // row ky belongs to group floor(ky G / kh)
       const int gb1 = g.G > 1 ? (a.kh + g.G - 1) / g.G : a.kh;
@@ -379,53 +384,56 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
         const uint32_t w_avd = desc_lo(s_base + L.a_vd + b * L.a_bytes, lbo_a);
         const uint32_t t_acc = tmem + tb * L.cols;
         const uint32_t t_corr = t_acc + g.G * kTN, t_den = t_acc + (g.G + 1) * kTN;
-        // Per kernel row: a few integer ops, then the MMAs (the thread's
-        // overhead between rows is time the tensor pipe may run dry).  The
-        // band-full wait needs no tcgen05 fence: the copy completes on the
-        // mbarrier itself.
-        for (int ky = 0; ky < a.kh; ++ky, ++u) {
-          const uint32_t s = u % kStages;
-          ok = wait_or_abort(&b_full[s], (u / kStages) & 1, &abort_flag, err_word, kDevErrMmaTimeout);
+        // Per ring stage one wait and one release; per kernel row a few
+        // integer ops, then the MMAs (the thread's overhead between rows is
+        // time the tensor pipe may run dry).  The band-full wait needs no
+        // tcgen05 fence: the copy completes on the mbarrier itself.
+        for (int ky0 = 0; ky0 < a.kh; ky0 += kRowsPerStage, ++u) {
+          const uint32_t s = u % L.nst;
+          ok = wait_or_abort(&b_full[s], (u / L.nst) & 1, &abort_flag, err_word, kDevErrMmaTimeout);
           if (!ok) break;
-          const int grp = (ky >= gb1) + (ky >= gb2);
-          const uint32_t f = (ky == 0 || ky == gb1 || ky == gb2) ? 0u : 1u;  // first row of its group
-          const uint32_t tg = t_acc + grp * kTN, td = t_den + grp * kTN;
-          // A_ky = the window advanced ky rows (16 bytes each); one k-step =
-          // two core matrices along K on both operands
-          uint32_t ah = w_ahi + ky, al = w_alo + ky, av = w_avd + ky;
-          uint32_t bh = w_ring + s * stage_w, bl = bh + g.NB * 8;
-          mma_bf16(tg, ah, bh, f);
-          mma_bf16(t_corr, ah, bl, ky != 0);
-          mma_bf16(t_corr, al, bh, 1u);
-          if (den_mma) {
-            mma_bf16(td, av, bh, f);
-            mma_bf16(td, av, bl, 1u);
-#pragma unroll 1
-            for (int ks = 1; ks < g.KS; ++ks) {
-              ah += a_ks;
-              al += a_ks;
-              av += a_ks;
-              bh += 16;
-              bl += 16;
-              mma_bf16(tg, ah, bh, 1u);
-              mma_bf16(t_corr, ah, bl, 1u);
-              mma_bf16(t_corr, al, bh, 1u);
-              mma_bf16(td, av, bh, 1u);
+          const int ky1 = min(a.kh, ky0 + kRowsPerStage);
+          for (int ky = ky0; ky < ky1; ++ky) {
+            const int grp = (ky >= gb1) + (ky >= gb2);
+            const uint32_t f = (ky == 0 || ky == gb1 || ky == gb2) ? 0u : 1u;  // first row of its group
+            const uint32_t tg = t_acc + grp * kTN, td = t_den + grp * kTN;
+            // A_ky = the window advanced ky rows (16 bytes each); one k-step =
+            // two core matrices along K on both operands
+            uint32_t ah = w_ahi + ky, al = w_alo + ky, av = w_avd + ky;
+            uint32_t bh = w_ring + s * stage_w + (ky - ky0) * row_w, bl = bh + g.NB * 8;
+            mma_bf16(tg, ah, bh, f);
+            mma_bf16(t_corr, ah, bl, ky != 0);
+            mma_bf16(t_corr, al, bh, 1u);
+            if (den_mma) {
+              mma_bf16(td, av, bh, f);
               mma_bf16(td, av, bl, 1u);
-            }
-          } else {
+#pragma unroll 1
+              for (int ks = 1; ks < g.KS; ++ks) {
+                ah += a_ks;
+                al += a_ks;
+                av += a_ks;
+                bh += 16;
+                bl += 16;
+                mma_bf16(tg, ah, bh, 1u);
+                mma_bf16(t_corr, ah, bl, 1u);
+                mma_bf16(t_corr, al, bh, 1u);
+                mma_bf16(td, av, bh, 1u);
+                mma_bf16(td, av, bl, 1u);
+              }
+            } else {
 #pragma unroll 2
-            for (int ks = 1; ks < g.KS; ++ks) {
-              ah += a_ks;
-              al += a_ks;
-              bh += 16;
-              bl += 16;
-              mma_bf16(tg, ah, bh, 1u);
-              mma_bf16(t_corr, ah, bl, 1u);
-              mma_bf16(t_corr, al, bh, 1u);
+              for (int ks = 1; ks < g.KS; ++ks) {
+                ah += a_ks;
+                al += a_ks;
+                bh += 16;
+                bl += 16;
+                mma_bf16(tg, ah, bh, 1u);
+                mma_bf16(t_corr, ah, bl, 1u);
+                mma_bf16(t_corr, al, bh, 1u);
+              }
             }
           }
-          mma_commit(&b_empty[s]);  // the band stage is free once these MMAs have read it
+          mma_commit(&b_empty[s]);  // the stage is free once these MMAs have read it
         }
         if (!ok) break;
         mma_commit(&a_empty[b]);
@@ -443,21 +451,24 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
       uint32_t u = 0;
       bool ok = true;
       for (int64_t t = blockIdx.x; t < total && ok; t += gridDim.x) {
-        for (int ky = 0; ky < a.kh; ++ky, ++u) {
-          const uint32_t s = u % kStages;
-          if (u >= kStages) {
-            ok = wait_or_abort(&b_empty[s], ((u / kStages) - 1) & 1, &abort_flag, err_word, kDevErrTmaTimeout);
+        for (int ky0 = 0; ky0 < a.kh; ky0 += kRowsPerStage, ++u) {
+          const uint32_t s = u % L.nst;
+          if (u >= static_cast<uint32_t>(L.nst)) {
+            ok = wait_or_abort(&b_empty[s], ((u / L.nst) - 1) & 1, &abort_flag, err_word, kDevErrTmaTimeout);
             if (!ok) break;
           }
-          mbar_arrive_expect_tx(&b_full[s], L.stage_bytes);
-          bulk_g2s(sm + L.ring + s * L.stage_bytes, a.bw_img + static_cast<size_t>(ky) * L.stage_bytes,
-                   L.stage_bytes, &b_full[s]);
+          // a tile's rows ky0 .. ky0+1 (fewer at the end) are contiguous in the image
+          const uint32_t bytes = static_cast<uint32_t>(min(kRowsPerStage, a.kh - ky0)) * L.row_bytes;
+          mbar_arrive_expect_tx(&b_full[s], bytes);
+          bulk_g2s(sm + L.ring + s * L.stage_bytes, a.bw_img + static_cast<size_t>(ky0) * L.row_bytes, bytes,
+                   &b_full[s]);
         }
       }
       if (!ok) {
         // every stage's newest copy must land before shared memory is released
-        for (uint32_t k = (u > kStages ? u - kStages : 0u); k < u; ++k)
-          mbar_wait_bounded(&b_full[k % kStages], (k / kStages) & 1, err_word, kDevErrTmaTimeout);
+        const uint32_t nst = static_cast<uint32_t>(L.nst);
+        for (uint32_t k = (u > nst ? u - nst : 0u); k < u; ++k)
+          mbar_wait_bounded(&b_full[k % nst], (k / nst) & 1, err_word, kDevErrTmaTimeout);
       }
     }
   } else {
@@ -812,15 +823,28 @@ __global__ void prep_tc_sat(const double* __restrict__ w64, int kh, int kw, doub
 
 }  // namespace
 
-static int tc_nbuf(int kh, int kw, bool has_nd) {
+constexpr uint32_t kSmemLimit = 227 * 1024 - 1024;  // less the 1024-byte alignment slack
+
+// Two A buffers (conversion overlaps the MMAs) with at least three ring
+// stages when they fit, else one A buffer; then as many stages as fit.
+static void tc_shape(int kh, int kw, bool has_nd, int* nbuf, int* nst) {
   const TcGeom g = make_geom(kh, kw);
-  return make_plan(g, has_nd, 2).total + 1024 <= 227 * 1024 ? 2 : 1;
+  for (int nb = 2; nb >= 1; --nb)
+    for (int st = kMaxStages; st >= (nb == 2 ? 3 : 2); --st)
+      if (make_plan(g, has_nd, nb, st).total <= kSmemLimit) {
+        *nbuf = nb;
+        *nst = st;
+        return;
+      }
+  *nbuf = 0;
+  *nst = 0;
 }
 
 int conv_tc_supported(int kh, int kw) {
   if (kh < 1 || kw < 1 || kh > kMaxTCK || kw > kMaxTCK) return 0;
   const TcGeom g = make_geom(kh, kw);
-  return make_plan(g, true, 1).total + 1024 <= 227 * 1024 && g.KW <= 128 && make_plan(g, true, 1).cols <= 512;
+  const TcPlan p = make_plan(g, true, 1, 2);
+  return p.total <= kSmemLimit && g.KW <= 128 && p.cols <= 512;
 }
 
 // Workspace: float64 weights | Toeplitz band images | summed-area table.
@@ -845,8 +869,10 @@ int run_conv_tc(const void* src, int dtype, int64_t H, int64_t W, int64_t pitch,
   double ndv = 0.0;
   const int kind = resolve_nodata(VSR_F32, nodata, nodata_kind, &ndv);
   const bool has_nd = kind != VSR_NODATA_NONE;
-  const int nbuf = tc_nbuf(kh, kw, has_nd);
-  const TcPlan L = make_plan(g, has_nd, nbuf);
+  int nbuf = 0, nst = 0;
+  tc_shape(kh, kw, has_nd, &nbuf, &nst);
+  if (!nbuf) return fail(VSR_ERR_UNSUPPORTED, "split-BF16 convolution: %dx%d kernel does not fit shared memory", kh, kw);
+  const TcPlan L = make_plan(g, has_nd, nbuf, nst);
   char* ws = static_cast<char*>(workspace);
   double* w64 = reinterpret_cast<double*>(ws);
   const size_t off_img = (static_cast<size_t>(kh) * kw * 8 + 255) & ~size_t(255);
@@ -862,7 +888,7 @@ int run_conv_tc(const void* src, int dtype, int64_t H, int64_t W, int64_t pitch,
   if (!err) return VSR_ERR_CUDA;
   const bool vec_out = out_dtype == VSR_F32 && aligned(dst, 16) && out_pitch % 4 == 0;
   TcArgs a{static_cast<const float*>(src), H, W, pitch, kind, static_cast<float>(ndv), nodata, dst, out_dtype,
-           out_pitch, vec_out ? 1 : 0, reinterpret_cast<const unsigned char*>(img), sat, w64, kh, kw, nbuf};
+           out_pitch, vec_out ? 1 : 0, reinterpret_cast<const unsigned char*>(img), sat, w64, kh, kw, nbuf, nst};
   // At least 116 KB of shared memory keeps one CTA (and its 512 TMEM columns) per SM.
   const size_t smem = std::max<size_t>(L.total + 1024, 116 * 1024);
   auto kern = kind == VSR_NODATA_NONE ? conv_tc_kernel<0> : (kind == VSR_NODATA_VALUE ? conv_tc_kernel<1> : conv_tc_kernel<2>);
