@@ -215,23 +215,20 @@ def run_vsr(args, ws, rank, local):
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # per-launch duration of the dominant kernel (one launch per step): an
+    # event pair around every launch of the timed region, read after it ends
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     e0.record(stream)
-    for _ in range(args.steps):
+    for i in range(args.steps):
+        ev[i][0].record(stream)
         step()
+        ev[i][1].record(stream)
     e1.record(stream)
     torch.cuda.synchronize()
     if ws > 1:
         torch.distributed.barrier()
     ms = e0.elapsed_time(e1)
-    # per-launch duration of the dominant kernel (one launch per step)
-    launch_ms = []
-    for _ in range(5):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        step()
-        b.record(stream)
-        b.synchronize()
-        launch_ms.append(a.elapsed_time(b))
+    launch_ms = [a.elapsed_time(b) for a, b in ev]
 
     # ---- end-to-end through the public API with host buffers ----
     host_in = torch.empty((H, W), dtype=torch.float32, pin_memory=True)
@@ -269,7 +266,7 @@ def run_vsr(args, ws, rank, local):
 
     if rank == 0:
         peak, peak_kind = _roofline_peak()
-        lmed = statistics.median(launch_ms)
+        lmed = statistics.mean(launch_ms)
         achieved = BYTES_PER_PX * px / (lmed * 1e-3) / 1e9
         traffic_file = ROOT / "profiles" / "horn_f32_tma_terrain16k_traffic.json"
         traffic = None
@@ -289,7 +286,7 @@ def run_vsr(args, ws, rank, local):
                        "l2": "inputs+outputs (3.5 GB/step) exceed L2; no flush",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
                        "autotuned": {"rows_per_tile": tuned["shape"][0], "tma_stages": tuned["shape"][1],
-                                     "threads_per_cta": tuned["shape"][2],
+                                     "threads_per_cta": tuned["shape"][2], "tma_store_tiles": tuned["shape"][3],
                                      "ms_by_config": {str(k): round(v, 4) for k, v in tuned["ms"].items()}}},
             "gpu_launches": args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -219,3 +219,47 @@ def test_terrain_16k_strips_vs_oracle(vsr):
         assert np.abs(h.astype(int) - rh_.astype(int)).max() <= 1
     del out, s_t, a_t, h_t
     torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("shape", [(300, 1000), (517, 1024), (64, 128)])
+def test_every_launch_config_gives_identical_results(vsr, shape):
+    """All autotuner configurations -- direct stores and TMA tensor stores,
+    every tile height -- write bit-identical outputs, on rasters whose edges
+    cut tiles and with nodata present."""
+    from vsr_gb300 import _lib
+
+    rng = np.random.default_rng(shape[0])
+    z = (1000 + rng.random(shape) * 50 + np.linspace(0, 900, shape[1])[None, :]).astype(np.float32)
+    z[rng.random(shape) < 0.01] = -9999.0
+    r = vsr.from_numpy(z, nodata=-9999.0, affine=(10.0, 0, 0, 0, -10.0, 0))
+    lib = _lib.load()
+    n = lib.vsr_tuning_count(_lib.VSR_OP_HORN)
+    assert n >= 7
+    ref = None
+    try:
+        for cfg in range(n):
+            _lib.check(lib.vsr_tuning_set(_lib.VSR_OP_HORN, cfg), "set")
+            out = vsr.raster_terrain(r)
+            got = {k: out[k].to_numpy().copy() for k in ("slope", "aspect", "hillshade")}
+            if ref is None:
+                ref = got
+                _check_terrain(vsr, z, r.affine, -9999.0)
+            else:
+                for k in got:
+                    np.testing.assert_array_equal(got[k], ref[k], err_msg=f"config {cfg} {k}")
+    finally:
+        _lib.check(lib.vsr_tuning_set(_lib.VSR_OP_HORN, 0), "set")
+
+
+def test_low_elevations_keep_aspect_accuracy(vsr):
+    """Near 0 m, neighbouring FP32 elevations differ by more than a factor of
+    two and their differences round; a small gradient built from them would
+    lose the 1e-4 degree aspect accuracy.  Those rows take exact gradients."""
+    shape = (517, 1024)
+    rng = np.random.default_rng(shape[0])
+    z = (rng.random(shape) * 50 + np.linspace(0, 900, shape[1])[None, :]).astype(np.float32)
+    z[rng.random(shape) < 0.01] = -9999.0
+    z[200:260, 300:400] = 0.0  # a flat sea-level patch with its coast
+    _check_terrain(vsr, z, (10.0, 0, 0, 0, -10.0, 0), -9999.0)
+    # the generic (unaligned) path as well
+    _check_terrain(vsr, np.ascontiguousarray(z[:, :1021]), (10.0, 0, 0, 0, -10.0, 0), -9999.0)

@@ -29,6 +29,7 @@
 //    hillshade stores.
 //  * horn_generic  -- every other dtype / alignment: one thread per pixel,
 //    clamped loads through L1.
+#include <type_traits>
 #include <vector>
 
 #include "vsr_internal.cuh"
@@ -147,6 +148,87 @@ __device__ __forceinline__ PixelOut horn_pixel(float gx, float gy, const HornPar
 
 constexpr int kWantSlope = 1, kWantAspect = 2, kWantHs = 4;
 
+// ---- the same arithmetic on pixel pairs with Blackwell's packed FP32
+// instructions (fma/mul/add .f32x2: two IEEE single-precision results per
+// instruction, rounded exactly as the scalar forms).  Selects, compares and
+// the MUFU approximations stay per element.  The fused kernel is
+// instruction-issue bound at about the HBM rate in scalar form; pairing
+// halves its FP instruction count.
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sel2(bool c0, bool c1, float2 a, float2 b) {
+  return make_float2(c0 ? a.x : b.x, c1 ? a.y : b.y);
+}
+
+__device__ __forceinline__ float2 atan_poly_deg2(float2 t) {
+  const float2 u = mul2(t, t);
+  float2 p = f2(-0.232309317f);
+  p = fma2(p, u, f2(1.2526542f));
+  p = fma2(p, u, f2(-3.20353885f));
+  p = fma2(p, u, f2(5.52457099f));
+  p = fma2(p, u, f2(-7.96905727f));
+  p = fma2(p, u, f2(11.4285402f));
+  p = fma2(p, u, f2(-19.0966035f));
+  p = fma2(p, u, f2(57.2957414f));
+  return mul2(t, p);
+}
+
+__device__ __forceinline__ float2 slope_deg2(float2 s) {
+  const float2 sp = add2(s, f2(1e-30f));
+  const float2 rs = make_float2(rsqrt_approx(sp.x), rsqrt_approx(sp.y));
+  const bool b0 = s.x > 1.0f, b1 = s.y > 1.0f;
+  const float2 t = sel2(b0, b1, rs, mul2(s, rs));
+  const float2 a = atan_poly_deg2(t);
+  return sel2(b0, b1, fma2(a, f2(-1.0f), f2(90.0f)), a);
+}
+
+__device__ __forceinline__ float2 aspect_deg2(float2 p, float2 q) {
+  const float ap0 = fabsf(p.x), aq0 = fabsf(q.x), ap1 = fabsf(p.y), aq1 = fabsf(q.y);
+  const bool w0 = aq0 > ap0, w1 = aq1 > ap1;
+  const float2 mx = make_float2(w0 ? aq0 : ap0, w1 ? aq1 : ap1);
+  const float2 mn = make_float2(w0 ? ap0 : aq0, w1 ? ap1 : aq1);
+  const float2 mxe = add2(mx, f2(1e-30f));
+  const float2 t = mul2(mn, make_float2(rcp_approx(mxe.x), rcp_approx(mxe.y)));
+  float2 a = atan_poly_deg2(t);
+  a = sel2(w0, w1, fma2(a, f2(-1.0f), f2(90.0f)), a);
+  a = sel2(p.x < 0.0f, p.y < 0.0f, fma2(a, f2(-1.0f), f2(180.0f)), a);
+  const float2 asp = fma2(make_float2(q.x > 0.0f ? 1.0f : -1.0f, q.y > 0.0f ? 1.0f : -1.0f), a, f2(90.0f));
+  return sel2(asp.x < 0.0f, asp.y < 0.0f, add2(asp, f2(360.0f)), asp);
+}
+
+__device__ __forceinline__ void hillshade_u8_2(float2 p, float2 q, float2 s, const HornParams& P, uint8_t& h0,
+                                               uint8_t& h1) {
+  const float2 num = fma2(f2(P.hs_a), p, fma2(f2(-P.hs_b), q, f2(P.cos_z)));
+  const float2 d = fma2(f2(P.zf2), s, f2(1.0f));
+  const float2 hr = mul2(num, make_float2(rsqrt_approx(d.x), rsqrt_approx(d.y)));
+  const float2 hs = make_float2(__saturatef(hr.x), __saturatef(hr.y));
+  const float2 v = fma2(hs, f2(255.0f), f2(0.5f));
+  h0 = static_cast<uint8_t>(__float2uint_rz(v.x));
+  h1 = static_cast<uint8_t>(__float2uint_rz(v.y));
+}
+
+// Two pixels: gradients (gx, gy) of pixel 0 in .x, pixel 1 in .y.
+template <int WANT>
+__device__ __forceinline__ void horn_px2(float2 gx, float2 gy, const HornParams& P, float& s0, float& s1, float& a0,
+                                         float& a1, uint8_t& h0, uint8_t& h1) {
+  const float2 p = mul2(gx, f2(P.inv8cx));
+  const float2 q = mul2(gy, f2(P.inv8cy));
+  const float2 s = fma2(p, p, mul2(q, q));
+  if (WANT & kWantSlope) {
+    const float2 v = slope_deg2(s);
+    s0 = v.x;
+    s1 = v.y;
+  }
+  if (WANT & kWantAspect) {
+    const float2 v = aspect_deg2(p, q);
+    a0 = v.x;
+    a1 = v.y;
+  }
+  if (WANT & kWantHs) hillshade_u8_2(p, q, s, P, h0, h1);
+}
+
 // The wanted outputs are a compile-time set, so the per-pixel path has no
 // branches on which outputs exist.
 template <int WANT>
@@ -159,6 +241,43 @@ __device__ __forceinline__ void horn_px(float gx, float gy, const HornParams& P,
   if (WANT & kWantHs) ho = hillshade_u8(p, q, s, P);
 }
 
+// ---- exact gradients.  Differences of neighbouring FP32 elevations are
+// exact when the operands lie within a factor of two of each other
+// (Sterbenz), which holds almost everywhere; near 0 m (or where values of
+// very different size meet, e.g. nodata) a difference can round, and a
+// small gradient formed from large rounded differences loses the aspect's
+// accuracy (the reference differences in float64).  Rows where that can
+// happen take error-free transformations instead: TwoDiff/TwoSum keep every
+// rounding error and the sum is formed to within one final rounding.
+__device__ __forceinline__ float2 two_diff(float a, float b) {  // s + e == a - b exactly
+  const float s = __fsub_rn(a, b);
+  const float z = __fsub_rn(s, a);
+  const float e = __fsub_rn(__fsub_rn(a, __fsub_rn(s, z)), __fadd_rn(b, z));
+  return make_float2(s, e);
+}
+__device__ __forceinline__ float2 two_sum(float a, float b) {  // s + e == a + b exactly
+  const float s = __fadd_rn(a, b);
+  const float z = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, z)), __fsub_rn(b, z));
+  return make_float2(s, e);
+}
+// (x2 - x0) + 2 (y2 - y0) + (z2 - z0), correctly rounded but for a tiny
+// fraction of an ulp; non-finite operands fall back to plain arithmetic.
+__device__ __forceinline__ float grad_exact(float x0, float x2, float y0, float y2, float z0, float z2) {
+  const float2 d1 = two_diff(x2, x0), d2 = two_diff(y2, y0), d3 = two_diff(z2, z0);
+  const float2 s12 = two_sum(d1.x, 2.0f * d2.x);
+  const float2 s = two_sum(s12.x, d3.x);
+  const float err = __fadd_rn(__fadd_rn(s12.y, s.y), __fadd_rn(__fadd_rn(d1.y, 2.0f * d2.y), d3.y));
+  const float g = __fadd_rn(s.x, err);
+  return fabsf(g) <= 3.402823466e38f ? g : fmaf(2.0f, y2 - y0, (x2 - x0) + (z2 - z0));
+}
+
+// Every difference (and the sums) of a row window is exact when all its
+// values lie in [m, 2m] for some m > 0, or in [-2m, -m], or are all zero.
+__device__ __forceinline__ bool window_exact(float lo, float hi) {
+  return (lo > 0.0f && hi <= 2.0f * lo) || (hi < 0.0f && lo >= 2.0f * hi) || (lo == 0.0f && hi == 0.0f);
+}
+
 // ------------------------------------------------------------ TMA kernel --
 constexpr int kTW = 128;        // output tile width (32 lanes x 4 pixels)
 constexpr int kSW = kTW + 8;    // staged width: 4-column halo each side (16 B)
@@ -168,6 +287,17 @@ struct TmaTile {
   static constexpr int SH = TH + 2;
   static constexpr uint32_t kBytes = kSW * SH * 4;
   static constexpr uint32_t kStride = (kBytes + 1023u) & ~1023u;
+};
+
+// Shared-memory output tile for TMA stores: slope and aspect TH x 128 f32,
+// hillshade TH x 128 u8 (only the wanted ones), 1024-byte aligned.
+template <int TH, int WANT>
+struct OutTile {
+  static constexpr uint32_t kSB = (WANT & 1) ? TH * kTW * 4 : 0;
+  static constexpr uint32_t kAB = (WANT & 2) ? TH * kTW * 4 : 0;
+  static constexpr uint32_t kHB = (WANT & 4) ? TH * kTW : 0;
+  static constexpr uint32_t kS = 0, kA = kSB, kH = kSB + kAB;
+  static constexpr uint32_t kBytes = (kSB + kAB + kHB + 1023u) & ~1023u;
 };
 
 __device__ __forceinline__ void load6(const float* row, int lane, float v[6]) {
@@ -194,35 +324,71 @@ __device__ __forceinline__ uint32_t nd_bits6(const float v[6], int kind, float n
 // Load one staged row for a lane: 6 values, its 4 horizontal differences
 // (x+2 minus x, shared by the three output rows that use the row) and, for
 // masked tiles, its 6 nodata bits.
+// Also the row's value range for the exactness test; with ``skip_nd``
+// nodata values are left out (their windows' outputs are masked).
 template <bool MASKED>
-__device__ __forceinline__ void stage_row(const float* row, int lane, const HornParams& P, float nd_in, float v[6],
-                                          float hd[4], uint32_t& m) {
+__device__ __forceinline__ void stage_row(const float* row, int lane, const HornParams& P, float nd_in, bool skip_nd,
+                                          float v[6], float hd[4], uint32_t& m, float& lo, float& hi) {
   load6(row, lane, v);
 #pragma unroll
   for (int k = 0; k < 4; ++k) hd[k] = v[k + 2] - v[k];
   m = MASKED ? nd_bits6(v, P.nd_kind, nd_in) : 0u;
+  if (MASKED && skip_nd && m) {
+    float l[6], h[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const bool nd = (m >> k) & 1u;
+      l[k] = nd ? __int_as_float(0x7f800000) : v[k];
+      h[k] = nd ? __int_as_float(0xff800000) : v[k];
+    }
+    lo = fminf(fminf(fminf(l[0], l[1]), fminf(l[2], l[3])), fminf(l[4], l[5]));
+    hi = fmaxf(fmaxf(fmaxf(h[0], h[1]), fmaxf(h[2], h[3])), fmaxf(h[4], h[5]));
+  } else {
+    lo = fminf(fminf(fminf(v[0], v[1]), fminf(v[2], v[3])), fminf(v[4], v[5]));
+    hi = fmaxf(fmaxf(fmaxf(v[0], v[1]), fmaxf(v[2], v[3])), fmaxf(v[4], v[5]));
+  }
 }
 
 // One output row (4 pixels of this lane) from the rows above (t) and below
 // (b), the three rows' horizontal differences and nodata bits.
-template <int WANT, bool MASKED, bool EDGE, bool VEC = true>
-__device__ __forceinline__ void horn_out_row(const float t[6], const float b[6], const float hdt[4],
-                                             const float hdm[4], const float hdb[4], uint32_t mt, uint32_t mm,
+// TO_SMEM: the row pointers address a shared-memory output tile (plain
+// stores; the streaming global stores below must not see a shared address).
+// Gradients of a lane's 4 pixels from the rows above (t), through (mid)
+// and below (b) and the rows' horizontal differences: the fast form from
+// the (exact) differences, or grad_exact where differences may round.
+__device__ __forceinline__ void grad_fast(const float t[6], const float b[6], const float hdt[4], const float hdm[4],
+                                          const float hdb[4], float gx[4], float gy[4]) {
+  float dv[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) dv[k] = b[k] - t[k];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    gx[k] = fmaf(2.0f, hdm[k], hdt[k] + hdb[k]);
+    gy[k] = fmaf(2.0f, dv[k + 1], dv[k] + dv[k + 2]);
+  }
+}
+
+__device__ __forceinline__ void grad_exact4(const float t[6], const float mid[6], const float b[6], float gx[4],
+                                            float gy[4]) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    gx[k] = grad_exact(t[k], t[k + 2], mid[k], mid[k + 2], b[k], b[k + 2]);
+    gy[k] = grad_exact(t[k], b[k], t[k + 1], b[k + 1], t[k + 2], b[k + 2]);
+  }
+}
+
+template <int WANT, bool MASKED, bool EDGE, bool VEC = true, bool TO_SMEM = false>
+__device__ __forceinline__ void horn_out_row(const float gx[4], const float gy[4], uint32_t mt, uint32_t mm,
                                              uint32_t mb, const HornParams& P, const MaskRule& rule, int64_t y,
                                              int64_t xs, float* __restrict__ srow, float* __restrict__ arow,
                                              uint8_t* __restrict__ hrow) {
   if (EDGE && (y >= P.height || xs >= P.width)) return;
-  float dv[6];
-#pragma unroll
-  for (int k = 0; k < 6; ++k) dv[k] = b[k] - t[k];
   float so[4], ao[4];
   uint8_t ho[4];
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const float gx = fmaf(2.0f, hdm[k], hdt[k] + hdb[k]);
-    const float gy = fmaf(2.0f, dv[k + 1], dv[k] + dv[k + 2]);
-    horn_px<WANT>(gx, gy, P, so[k], ao[k], ho[k]);
-  }
+  for (int k = 0; k < 4; k += 2)
+    horn_px2<WANT>(make_float2(gx[k], gx[k + 1]), make_float2(gy[k], gy[k + 1]), P, so[k], so[k + 1], ao[k],
+                   ao[k + 1], ho[k], ho[k + 1]);
   if (MASKED) {
     const uint32_t hdil = (mt | (mt >> 1) | (mt >> 2)) | (mm | (mm >> 1) | (mm >> 2)) | (mb | (mb >> 1) | (mb >> 2));
     const uint32_t sabits = rule.sa_any ? (rule.sa_center ? (mm >> 1) : hdil) : 0u;
@@ -236,7 +402,13 @@ __device__ __forceinline__ void horn_out_row(const float t[6], const float b[6],
     }
   }
   const bool full = VEC && (!EDGE || xs + 3 < P.width);
-  if (full) {
+  if (TO_SMEM) {
+    if (WANT & kWantSlope) *reinterpret_cast<float4*>(srow) = make_float4(so[0], so[1], so[2], so[3]);
+    if (WANT & kWantAspect) *reinterpret_cast<float4*>(arow) = make_float4(ao[0], ao[1], ao[2], ao[3]);
+    if (WANT & kWantHs)
+      *reinterpret_cast<unsigned int*>(hrow) =
+          uint32_t(ho[0]) | (uint32_t(ho[1]) << 8) | (uint32_t(ho[2]) << 16) | (uint32_t(ho[3]) << 24);
+  } else if (full) {
     if (WANT & kWantSlope) __stcs(reinterpret_cast<float4*>(srow), make_float4(so[0], so[1], so[2], so[3]));
     if (WANT & kWantAspect) __stcs(reinterpret_cast<float4*>(arow), make_float4(ao[0], ao[1], ao[2], ao[3]));
     if (WANT & kWantHs)
@@ -257,34 +429,49 @@ __device__ __forceinline__ void horn_out_row(const float t[6], const float b[6],
 // RB output rows of one warp: rows r0 .. r0+RB-1 of the tile (staged rows
 // r0 .. r0+RB+1), lane columns xs .. xs+3.  Two output rows per iteration
 // (rolled on purpose: a fully unrolled loop overflowed the instruction cache).
-template <int RB, int WANT, bool MASKED, bool EDGE, bool VEC = true>
+// ``srow``/``arow``/``hrow`` point at this lane's first output pixel (global
+// memory, or a shared-memory staging tile for TMA stores); ``sp``/``hp``
+// are their row pitches in elements.
+template <int RB, int WANT, bool MASKED, bool EDGE, bool VEC = true, bool TO_SMEM = false>
 __device__ __forceinline__ void horn_rows(const float* S, int lane, int r0, int64_t y0, int64_t xs,
                                           const HornParams& P, const MaskRule& rule, float nd_in,
-                                          float* __restrict__ slope, float* __restrict__ aspect,
-                                          uint8_t* __restrict__ hs) {
+                                          float* __restrict__ srow, float* __restrict__ arow,
+                                          uint8_t* __restrict__ hrow, int64_t sp, int64_t hp) {
   static_assert(RB % 2 == 0, "two output rows per iteration");
   float v0[6], v1[6], hd0[4], hd1[4];
   uint32_t m0, m1;
-  stage_row<MASKED>(S + (r0 + 0) * kSW, lane, P, nd_in, v0, hd0, m0);
-  stage_row<MASKED>(S + (r0 + 1) * kSW, lane, P, nd_in, v1, hd1, m1);
+  float lo0, hi0, lo1, hi1;
+  // nodata values may be left out of the exactness test when every output
+  // whose window holds one is masked (3x3 dilation; not the centre-only rule)
+  const bool skip_nd = !rule.sa_center;
+  stage_row<MASKED>(S + (r0 + 0) * kSW, lane, P, nd_in, skip_nd, v0, hd0, m0, lo0, hi0);
+  stage_row<MASKED>(S + (r0 + 1) * kSW, lane, P, nd_in, skip_nd, v1, hd1, m1, lo1, hi1);
   const int64_t y = y0 + r0;
-  float* srow = (WANT & kWantSlope) ? slope + y * P.out_pitch + xs : nullptr;
-  float* arow = (WANT & kWantAspect) ? aspect + y * P.out_pitch + xs : nullptr;
-  uint8_t* hrow = (WANT & kWantHs) ? hs + y * P.hs_pitch + xs : nullptr;
 #pragma unroll 1
   for (int j = 0; j < RB; j += 2) {
     float v2[6], v3[6], hd2[4], hd3[4];
     uint32_t m2, m3;
-    stage_row<MASKED>(S + (r0 + j + 2) * kSW, lane, P, nd_in, v2, hd2, m2);
-    stage_row<MASKED>(S + (r0 + j + 3) * kSW, lane, P, nd_in, v3, hd3, m3);
-    horn_out_row<WANT, MASKED, EDGE, VEC>(v0, v2, hd0, hd1, hd2, m0, m1, m2, P, rule, y + j, xs, srow, arow, hrow);
-    if (WANT & kWantSlope) srow += P.out_pitch;
-    if (WANT & kWantAspect) arow += P.out_pitch;
-    if (WANT & kWantHs) hrow += P.hs_pitch;
-    horn_out_row<WANT, MASKED, EDGE, VEC>(v1, v3, hd1, hd2, hd3, m1, m2, m3, P, rule, y + j + 1, xs, srow, arow, hrow);
-    if (WANT & kWantSlope) srow += P.out_pitch;
-    if (WANT & kWantAspect) arow += P.out_pitch;
-    if (WANT & kWantHs) hrow += P.hs_pitch;
+    float lo2, hi2, lo3, hi3;
+    stage_row<MASKED>(S + (r0 + j + 2) * kSW, lane, P, nd_in, skip_nd, v2, hd2, m2, lo2, hi2);
+    stage_row<MASKED>(S + (r0 + j + 3) * kSW, lane, P, nd_in, skip_nd, v3, hd3, m3, lo3, hi3);
+    // both output rows of the pair take the exact form if any lane's window may round
+    const float lo = fminf(fminf(lo0, lo1), fminf(lo2, lo3)), hi = fmaxf(fmaxf(hi0, hi1), fmaxf(hi2, hi3));
+    float* srow1 = (WANT & kWantSlope) ? srow + sp : nullptr;
+    float* arow1 = (WANT & kWantAspect) ? arow + sp : nullptr;
+    uint8_t* hrow1 = (WANT & kWantHs) ? hrow + hp : nullptr;
+    float gxa[4], gya[4], gxb[4], gyb[4];
+    if (__all_sync(0xffffffffu, window_exact(lo, hi))) {
+      grad_fast(v0, v2, hd0, hd1, hd2, gxa, gya);
+      grad_fast(v1, v3, hd1, hd2, hd3, gxb, gyb);
+    } else {
+      grad_exact4(v0, v1, v2, gxa, gya);
+      grad_exact4(v1, v2, v3, gxb, gyb);
+    }
+    horn_out_row<WANT, MASKED, EDGE, VEC, TO_SMEM>(gxa, gya, m0, m1, m2, P, rule, y + j, xs, srow, arow, hrow);
+    horn_out_row<WANT, MASKED, EDGE, VEC, TO_SMEM>(gxb, gyb, m1, m2, m3, P, rule, y + j + 1, xs, srow1, arow1, hrow1);
+    if (WANT & kWantSlope) srow = srow1 + sp;
+    if (WANT & kWantAspect) arow = arow1 + sp;
+    if (WANT & kWantHs) hrow = hrow1 + hp;
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
       v0[k] = v2[k];
@@ -297,23 +484,50 @@ __device__ __forceinline__ void horn_rows(const float* S, int lane, int r0, int6
     }
     m0 = m2;
     m1 = m3;
+    lo0 = lo2;
+    hi0 = hi2;
+    lo1 = lo3;
+    hi1 = hi3;
   }
 }
 
-template <int TH, int STAGES, int THREADS, int WANT>
-__global__ void __launch_bounds__(THREADS, 768 / THREADS) horn_f32_tma(const __grid_constant__ CUtensorMap tmap,
+// This lane's first output pixel of rows starting at y in global memory.
+struct RowPtrs {
+  float* s;
+  float* a;
+  uint8_t* h;
+};
+__device__ __forceinline__ RowPtrs global_rows(float* slope, float* aspect, uint8_t* hs, const HornParams& P,
+                                               int64_t y, int64_t xs) {
+  return {slope ? slope + y * P.out_pitch + xs : nullptr, aspect ? aspect + y * P.out_pitch + xs : nullptr,
+          hs ? hs + y * P.hs_pitch + xs : nullptr};
+}
+
+// OB = 0: each lane stores its results straight to global memory.  OB >= 1:
+// results go to OB shared-memory output tiles that one thread writes back
+// with TMA tensor stores (bulk groups; a tile is rewritten only after its
+// store has finished reading it).  The copy engine keeps far more writes in
+// flight than the CTA's threads can, and the kernel's traffic is two thirds
+// writes.
+template <int TH, int STAGES, int THREADS, int WANT, int OB, int MINB = 768 / THREADS>
+__global__ void __launch_bounds__(THREADS, MINB) horn_f32_tma(const __grid_constant__ CUtensorMap tmap,
+                                                        const __grid_constant__ CUtensorMap smap,
+                                                        const __grid_constant__ CUtensorMap amap,
+                                                        const __grid_constant__ CUtensorMap hmap,
                                                         const HornParams P, const float nd_in,
                                                         float* __restrict__ slope,
                                                         float* __restrict__ aspect,
                                                         uint8_t* __restrict__ hs,
                                                         uint32_t* err_word) {
   using Tile = TmaTile<TH>;
+  using Out = OutTile<TH, WANT>;
   constexpr int WARPS = THREADS / 32;
   constexpr int RB = TH / WARPS;  // output rows per warp
   static_assert(RB * WARPS == TH, "TH must be a multiple of the warp count");
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bars[STAGES];
   float* stages = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  unsigned char* out_base = reinterpret_cast<unsigned char*>(stages) + STAGES * Tile::kStride;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t W = P.width, H = P.height;
@@ -346,7 +560,10 @@ __global__ void __launch_bounds__(THREADS, 768 / THREADS) horn_f32_tma(const __g
     const int s = static_cast<int>(it % STAGES);
     const uint32_t parity = static_cast<uint32_t>((it / STAGES) & 1);
     const bool ok = mbar_wait_bounded(&bars[s], parity, err_word, kDevErrTmaTimeout);
+    // output tile it % OB is rewritten below: its previous store must have read it
+    if (OB > 0 && tid == 0) bulk_wait_read<OB - 1>();
     if (__syncthreads_or(!ok)) {
+      if (OB > 0 && tid == 0) bulk_wait_read<0>();
       // Give the other copies in flight a bounded chance to land before the
       // CTA's shared memory is released, then leave.
       if (tid == 0) {
@@ -396,16 +613,37 @@ __global__ void __launch_bounds__(THREADS, 768 / THREADS) horn_f32_tma(const __g
     const bool masked = __syncthreads_or(any_nd);
 
     const int64_t xs = x0 + 4 * lane;
-    const bool edge = x0 + kTW > W || y0 + TH > H;
-    if (masked) {
-      if (edge) horn_rows<RB, WANT, true, true>(S, lane, warp * RB, y0, xs, P, rule, nd_in, slope, aspect, hs);
-      else horn_rows<RB, WANT, true, false>(S, lane, warp * RB, y0, xs, P, rule, nd_in, slope, aspect, hs);
+    const int r0 = warp * RB;
+    if (OB > 0) {
+      // whole tile into shared memory (pixels past the raster edge are
+      // computed from the replicated halo and clipped by the tensor store)
+      unsigned char* ob = out_base + static_cast<uint32_t>(it % (OB > 0 ? OB : 1)) * Out::kBytes;
+      float* so = reinterpret_cast<float*>(ob + Out::kS) + r0 * kTW + 4 * lane;
+      float* ao = reinterpret_cast<float*>(ob + Out::kA) + r0 * kTW + 4 * lane;
+      uint8_t* ho = ob + Out::kH + r0 * kTW + 4 * lane;
+      if (masked) horn_rows<RB, WANT, true, false, true, true>(S, lane, r0, y0, xs, P, rule, nd_in, so, ao, ho, kTW, kTW);
+      else horn_rows<RB, WANT, false, false, true, true>(S, lane, r0, y0, xs, P, rule, nd_in, so, ao, ho, kTW, kTW);
+      fence_proxy_async_smem();  // generic-proxy tile writes -> visible to the tensor store
     } else {
-      if (edge) horn_rows<RB, WANT, false, true>(S, lane, warp * RB, y0, xs, P, rule, nd_in, slope, aspect, hs);
-      else horn_rows<RB, WANT, false, false>(S, lane, warp * RB, y0, xs, P, rule, nd_in, slope, aspect, hs);
+      const bool edge = x0 + kTW > W || y0 + TH > H;
+      const RowPtrs g = global_rows(slope, aspect, hs, P, y0 + r0, xs);
+      if (masked) {
+        if (edge) horn_rows<RB, WANT, true, true>(S, lane, r0, y0, xs, P, rule, nd_in, g.s, g.a, g.h, P.out_pitch, P.hs_pitch);
+        else horn_rows<RB, WANT, true, false>(S, lane, r0, y0, xs, P, rule, nd_in, g.s, g.a, g.h, P.out_pitch, P.hs_pitch);
+      } else {
+        if (edge) horn_rows<RB, WANT, false, true>(S, lane, r0, y0, xs, P, rule, nd_in, g.s, g.a, g.h, P.out_pitch, P.hs_pitch);
+        else horn_rows<RB, WANT, false, false>(S, lane, r0, y0, xs, P, rule, nd_in, g.s, g.a, g.h, P.out_pitch, P.hs_pitch);
+      }
     }
 
-    __syncthreads();  // every read of stage s is done
+    __syncthreads();  // every read of stage s (and every write of the output tile) is done
+    if (OB > 0 && tid == 0) {
+      const unsigned char* ob = out_base + static_cast<uint32_t>(it % (OB > 0 ? OB : 1)) * Out::kBytes;
+      if (WANT & kWantSlope) tma_store_2d(&smap, static_cast<int>(x0), static_cast<int>(y0), ob + Out::kS);
+      if (WANT & kWantAspect) tma_store_2d(&amap, static_cast<int>(x0), static_cast<int>(y0), ob + Out::kA);
+      if (WANT & kWantHs) tma_store_2d(&hmap, static_cast<int>(x0), static_cast<int>(y0), ob + Out::kH);
+      bulk_commit();
+    }
     if (tid == 0) {
       const int64_t nt = t + static_cast<int64_t>(STAGES) * gridDim.x;
       if (nt < total) {
@@ -414,6 +652,7 @@ __global__ void __launch_bounds__(THREADS, 768 / THREADS) horn_f32_tma(const __g
       }
     }
   }
+  if (OB > 0 && tid == 0) bulk_wait_read<0>();  // the last stores must read the tiles before the CTA exits
 }
 
 // -------------------------------------------------------- generic kernel --
@@ -450,8 +689,14 @@ __global__ void __launch_bounds__(256) horn_generic(const T* __restrict__ src, c
       v[r][c] = static_cast<D>(t);
     }
   }
-  const float gx = static_cast<float>((v[0][2] - v[0][0]) + D(2) * (v[1][2] - v[1][0]) + (v[2][2] - v[2][0]));
-  const float gy = static_cast<float>((v[2][0] - v[0][0]) + D(2) * (v[2][1] - v[0][1]) + (v[2][2] - v[0][2]));
+  float gx, gy;
+  if constexpr (std::is_same<T, float>::value) {  // float differences may round (see grad_exact)
+    gx = grad_exact(v[0][0], v[0][2], v[1][0], v[1][2], v[2][0], v[2][2]);
+    gy = grad_exact(v[0][0], v[2][0], v[0][1], v[2][1], v[0][2], v[2][2]);
+  } else {  // exact: small integers in float, wider types in double
+    gx = static_cast<float>((v[0][2] - v[0][0]) + D(2) * (v[1][2] - v[1][0]) + (v[2][2] - v[2][0]));
+    gy = static_cast<float>((v[2][0] - v[0][0]) + D(2) * (v[2][1] - v[0][1]) + (v[2][2] - v[0][2]));
+  }
   const PixelOut o = horn_pixel(gx, gy, P, slope != nullptr, aspect != nullptr, hs != nullptr);
   const bool sa_nd = rule.sa_any && (rule.sa_center ? ctr : dil);
   if (slope) slope[y * P.out_pitch + x] = sa_nd ? nd_out<O>(P) : static_cast<O>(o.slope);
@@ -486,44 +731,67 @@ int dispatch_generic(int dtype, const void* src, const HornParams& P, double ndv
   }
 }
 
-template <int TH, int STAGES, int THREADS, int WANT>
+template <int TH, int STAGES, int THREADS, int WANT, int OB, int MINB = 768 / THREADS>
 int launch_tma(const void* src, const HornParams& P, float nd_in, float* slope, float* aspect,
                uint8_t* hs, cudaStream_t st) {
   using Tile = TmaTile<TH>;
-  CUtensorMap map;
+  using Out = OutTile<TH, WANT>;
+  if (OB > 0 && hs && (!aligned(hs, 16) || P.hs_pitch % 16 != 0))  // tensor-store rows need 16-byte strides
+    return launch_tma<TH, STAGES, THREADS, WANT, 0, MINB>(src, P, nd_in, slope, aspect, hs, st);
+  CUtensorMap map, smap, amap, hmap;
   int rc = encode_tensor_map_2d(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, src, P.width, P.height,
                                 P.in_pitch, kSW, Tile::SH);
   if (rc) return rc;
+  smap = amap = hmap = map;  // unused output maps are never read
+  if (OB > 0) {
+    if (slope && (rc = encode_tensor_map_2d(&smap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, slope, P.width, P.height,
+                                            P.out_pitch, kTW, TH)))
+      return rc;
+    if (aspect && (rc = encode_tensor_map_2d(&amap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, aspect, P.width, P.height,
+                                             P.out_pitch, kTW, TH)))
+      return rc;
+    if (hs && (rc = encode_tensor_map_2d(&hmap, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, hs, P.width, P.height, P.hs_pitch,
+                                         kTW, TH)))
+      return rc;
+  }
   uint32_t* err = device_error_word();
   if (!err) return VSR_ERR_CUDA;
-  const size_t smem = STAGES * Tile::kStride + 1024;
-  auto kern = horn_f32_tma<TH, STAGES, THREADS, WANT>;
+  const size_t smem = STAGES * Tile::kStride + OB * Out::kBytes + 1024;
+  auto kern = horn_f32_tma<TH, STAGES, THREADS, WANT, OB, MINB>;
   VSR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   int per_sm = 0;
   VSR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, THREADS, smem));
   if (per_sm < 1) return fail(VSR_ERR_CUDA, "horn_f32_tma cannot be resident (smem %zu)", smem);
   const int64_t tiles = ((P.width + kTW - 1) / kTW) * ((P.height + TH - 1) / TH);
   const int64_t grid = std::min<int64_t>(tiles, static_cast<int64_t>(sm_count()) * per_sm);
-  kern<<<static_cast<unsigned>(grid), THREADS, smem, st>>>(map, P, nd_in, slope, aspect, hs, err);
+  kern<<<static_cast<unsigned>(grid), THREADS, smem, st>>>(map, smap, amap, hmap, P, nd_in, slope, aspect, hs, err);
   VSR_CUDA_TRY(cudaGetLastError());
   return VSR_OK;
 }
 
 // Launch configurations of the TMA kernel the autotuner chooses between:
-// (output rows per tile, pipeline stages, threads per CTA).
+// (output rows per tile, pipeline stages, threads per CTA, shared-memory
+// output tiles for TMA stores; 0 = direct stores).
 struct HornConfig {
-  int th, stages, threads;
+  int th, stages, threads, ob, minb;  // minb: CTAs per SM the register budget is sized for
 };
-constexpr HornConfig kHornConfigs[] = {{64, 2, 256}, {32, 2, 128}, {32, 3, 256}};
+constexpr HornConfig kHornConfigs[] = {{64, 2, 128, 0, 4}, {32, 2, 128, 0, 4}, {32, 2, 128, 0, 5},
+                                       {32, 2, 128, 0, 6}, {64, 2, 256, 0, 3}, {32, 3, 128, 0, 4},
+                                       {32, 2, 256, 2, 3}, {16, 2, 256, 2, 3}};
 constexpr int kNumHornConfigs = sizeof(kHornConfigs) / sizeof(kHornConfigs[0]);
 
 template <int WANT>
 int launch_tma_want(int cfg, const void* src, const HornParams& P, float nd_in, float* slope, float* aspect,
                     uint8_t* hs, cudaStream_t st) {
   switch (cfg) {
-    case 1: return launch_tma<32, 2, 128, WANT>(src, P, nd_in, slope, aspect, hs, st);
-    case 2: return launch_tma<32, 3, 256, WANT>(src, P, nd_in, slope, aspect, hs, st);
-    default: return launch_tma<64, 2, 256, WANT>(src, P, nd_in, slope, aspect, hs, st);
+    case 1: return launch_tma<32, 2, 128, WANT, 0, 4>(src, P, nd_in, slope, aspect, hs, st);
+    case 2: return launch_tma<32, 2, 128, WANT, 0, 5>(src, P, nd_in, slope, aspect, hs, st);
+    case 3: return launch_tma<32, 2, 128, WANT, 0, 6>(src, P, nd_in, slope, aspect, hs, st);
+    case 4: return launch_tma<64, 2, 256, WANT, 0, 3>(src, P, nd_in, slope, aspect, hs, st);
+    case 5: return launch_tma<32, 3, 128, WANT, 0, 4>(src, P, nd_in, slope, aspect, hs, st);
+    case 6: return launch_tma<32, 2, 256, WANT, 2, 3>(src, P, nd_in, slope, aspect, hs, st);
+    case 7: return launch_tma<16, 2, 256, WANT, 2, 3>(src, P, nd_in, slope, aspect, hs, st);
+    default: return launch_tma<64, 2, 128, WANT, 0, 4>(src, P, nd_in, slope, aspect, hs, st);
   }
 }
 
@@ -760,18 +1028,19 @@ __global__ void __launch_bounds__(THREADS) batch_terrain_kernel(BatchHeader* __r
     if (T.slope || T.aspect) {
       const int64_t xs = x0 + 4 * lane;
       const float* Sh = S + (HY - 1) * kSW;
+      const RowPtrs g = global_rows(T.slope, T.aspect, nullptr, P, y0 + warp * RB, xs);
       // both outputs are requested together in the batch plan
       if (T.vec) {
         if (masked) {
-          if (edge) horn_rows<RB, 3, true, true, true>(Sh, lane, warp * RB, y0, xs, P, rule, nd_in, T.slope, T.aspect, nullptr);
-          else horn_rows<RB, 3, true, false, true>(Sh, lane, warp * RB, y0, xs, P, rule, nd_in, T.slope, T.aspect, nullptr);
+          if (edge) horn_rows<RB, 3, true, true, true>(Sh, lane, warp * RB, y0, xs, P, rule, nd_in, g.s, g.a, g.h, P.out_pitch, P.hs_pitch);
+          else horn_rows<RB, 3, true, false, true>(Sh, lane, warp * RB, y0, xs, P, rule, nd_in, g.s, g.a, g.h, P.out_pitch, P.hs_pitch);
         } else {
-          if (edge) horn_rows<RB, 3, false, true, true>(Sh, lane, warp * RB, y0, xs, P, rule, nd_in, T.slope, T.aspect, nullptr);
-          else horn_rows<RB, 3, false, false, true>(Sh, lane, warp * RB, y0, xs, P, rule, nd_in, T.slope, T.aspect, nullptr);
+          if (edge) horn_rows<RB, 3, false, true, true>(Sh, lane, warp * RB, y0, xs, P, rule, nd_in, g.s, g.a, g.h, P.out_pitch, P.hs_pitch);
+          else horn_rows<RB, 3, false, false, true>(Sh, lane, warp * RB, y0, xs, P, rule, nd_in, g.s, g.a, g.h, P.out_pitch, P.hs_pitch);
         }
       } else {
-        if (masked) horn_rows<RB, 3, true, true, false>(Sh, lane, warp * RB, y0, xs, P, rule, nd_in, T.slope, T.aspect, nullptr);
-        else horn_rows<RB, 3, false, true, false>(Sh, lane, warp * RB, y0, xs, P, rule, nd_in, T.slope, T.aspect, nullptr);
+        if (masked) horn_rows<RB, 3, true, true, false>(Sh, lane, warp * RB, y0, xs, P, rule, nd_in, g.s, g.a, g.h, P.out_pitch, P.hs_pitch);
+        else horn_rows<RB, 3, false, true, false>(Sh, lane, warp * RB, y0, xs, P, rule, nd_in, g.s, g.a, g.h, P.out_pitch, P.hs_pitch);
       }
     }
 
