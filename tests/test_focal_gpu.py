@@ -144,3 +144,35 @@ def test_focal_mean_known_answer(vsr):
     out = vsr.raster_focal_mean(vsr.from_numpy(d), 1).to_numpy()
     assert out[2, 2] == 13.0
     assert any(e.detail.startswith("gpu_focal_mean") for e in vsr.raster_focal_mean(vsr.from_numpy(d), 1).diagnostics)
+
+
+@pytest.mark.parametrize("dtype,r", [(np.uint16, 3), (np.int16, 7), (np.uint8, 5), (np.uint16, 1)])
+def test_focal_mean_integer_sliding_window(vsr, dtype, r):
+    """Square windows on 8/16-bit rasters (the packed sliding-window kernel):
+    several 256-row strips and 128-column blocks with ragged edges, odd row
+    pitch (no paired loads) and even pitch, exact float64 means and correctly
+    rounded float32 means."""
+    rng = np.random.default_rng(r)
+    lo, hi = {np.uint16: (0, 65535), np.int16: (-32767, 32767), np.uint8: (0, 254)}[dtype]
+    nd = {np.uint16: 0, np.int16: -32768, np.uint8: 255}[dtype]
+    for shape in [(600, 389), (300, 1024)]:
+        d = rng.integers(lo, hi, shape, endpoint=True).astype(dtype)
+        d[rng.random(shape) < 0.03] = nd
+        d[:20, :30] = nd  # a window with no valid value
+        ref = oracle.focal_mean(d, r, r, nd)
+        r_ = vsr.from_numpy(d, nodata=nd)
+        np.testing.assert_array_equal(vsr.raster_focal_mean(r_, r).to_numpy(), ref)
+        out32 = vsr.raster_focal_mean(r_, r, out_dtype=np.float32).to_numpy()
+        np.testing.assert_array_equal(out32, ref.astype(np.float32))
+
+
+def test_focal_mean_multiband_uint16_equals_per_band(vsr):
+    from vsr_gb300 import algebra
+
+    rng = np.random.default_rng(11)
+    stack = rng.integers(0, 10000, (3, 270, 300)).astype(np.uint16)
+    stack[rng.random(stack.shape) < 0.03] = 0
+    r = vsr.from_numpy(stack, nodata=0)
+    allb = algebra.focal_mean_bands(r, 3, 3, out_dtype=np.float32).cpu().numpy()
+    for i in range(3):
+        np.testing.assert_array_equal(allb[i], oracle.focal_mean(stack[i], 3, 3, 0).astype(np.float32))

@@ -19,6 +19,7 @@
 //   mean = sum / count formed in float64 (reference: Welford in float64,
 //   kernels/focal.py:672-769 / scipy generic_filter, algebra.py:3083-3101).
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 
 #include "vsr_internal.cuh"
@@ -918,6 +919,206 @@ int launch_box_fast(const BoxArgs& a, cudaStream_t st, int bands) {
   return VSR_OK;
 }
 
+// ------------------------------------------------------- box_slide_int --
+// Focal mean of 8/16-bit integer rasters with a square (2R+1)^2 window,
+// R <= 7: the C5 multiband workload (12 x 10980^2 uint16, 7 x 7).
+//
+// Each tap is packed into one 32-bit word, value (offset to be
+// non-negative) in the low bits and a count bit above them:
+//   p = valid ? (v + off) | 1 << S : 0,
+// so one integer add sums value and count together and every sum is exact.
+// A block owns 128 columns (one per thread) and a strip of 256 rows.  Input
+// rows stream through a two-slot shared-memory ring (16 rows a slot, loaded
+// into registers one slot ahead); each thread forms the horizontal window
+// sum of its column per input row and slides the vertical window with a
+// register shift register (add the entering row, subtract the leaving one).
+// mean = (sum - off count) / count, one correctly rounded division.
+template <int R>
+struct SlidePack {
+  static constexpr int kTaps = (2 * R + 1) * (2 * R + 1);
+  // value-sum bits: the smallest S with taps * 65535 < 2^S
+  static constexpr int kShift = kTaps * 65535ll < (1ll << 22) ? 22 : (kTaps * 65535ll < (1ll << 23) ? 23 : 24);
+  static_assert(kTaps * 65535ll < (1ll << kShift), "value sum overflows the low field");
+  static_assert(kTaps < (1 << (32 - kShift)), "count overflows the high field");
+};
+
+constexpr int kSlTW = 128;               // output columns per block
+constexpr int kSlHalo = 8;               // staged columns each side (R <= 7, even for pair loads)
+constexpr int kSlSW = kSlTW + 2 * kSlHalo;  // 144 staged elements per row
+constexpr int kSlCH = 16;                // rows per ring slot
+constexpr int kSlStrip = 256;            // output rows per block
+constexpr int kSlWords = kSlCH * kSlSW / 2;  // element pairs per slot
+constexpr int kSlPer = (kSlWords + kSlTW - 1) / kSlTW;  // pairs per thread per slot
+
+template <int R, typename T, bool PAIR>
+__global__ void __launch_bounds__(kSlTW) box_slide_int(const BoxArgs a) {
+  using Pk = SlidePack<R>;
+  constexpr int OFF = std::is_signed<T>::value ? 32768 : 0;
+  constexpr uint32_t kOne = 1u << Pk::kShift, kLow = kOne - 1u;
+  __shared__ uint32_t ring[2][kSlCH][kSlSW];
+  const int c = threadIdx.x;
+  const int64_t x0 = static_cast<int64_t>(blockIdx.x) * kSlTW;
+  const int64_t ys = static_cast<int64_t>(blockIdx.y) * kSlStrip;
+  const T* src = static_cast<const T*>(band_src(a.src, a.dtype, a.band_stride));
+  void* dst = band_dst(a.dst, a.out_dtype, a.out_band_stride);
+  const int64_t nout = a.H - ys < kSlStrip ? a.H - ys : static_cast<int64_t>(kSlStrip);
+  const int nin = static_cast<int>(nout) + 2 * R;  // input rows ys - R .. ys + nout + R - 1
+  const int nchunks = (nin + kSlCH - 1) / kSlCH;
+  const bool has_nd = a.nd.kind == VSR_NODATA_VALUE;
+  const int64_t ndv = a.nd.iv;
+
+  auto pack = [&](uint32_t e, bool inb) -> uint32_t {
+    const T v = static_cast<T>(e);
+    const bool ok = inb && !(has_nd && static_cast<int64_t>(v) == ndv);
+    return ok ? ((static_cast<uint32_t>(static_cast<int>(v) + OFF)) | kOne) : 0u;
+  };
+  // Element pairs of a slot: pair w -> staged row w / (kSlSW / 2), columns
+  // 2 (w % (kSlSW / 2)) and +1.  A thread's pairs sit at the same columns
+  // in every chunk: their offsets and column bounds are fixed up front.
+  // Loads go to raw registers one chunk ahead; packing happens at the store
+  // (a load's value is not needed until then).
+  int64_t coff[kSlPer];
+  int prow[kSlPer];
+  uint32_t colin = 0u;  // 2 bits per pair: element in [0, W)
+#pragma unroll
+  for (int i = 0; i < kSlPer; ++i) {
+    const int w = c + kSlTW * i;
+    prow[i] = w < kSlWords ? w / (kSlSW / 2) : -1;
+    const int wc = w - (w / (kSlSW / 2)) * (kSlSW / 2);
+    const int64_t gx = x0 - kSlHalo + 2 * wc;
+    coff[i] = gx;
+    colin |= (static_cast<uint32_t>(gx >= 0 && gx < a.W) | (static_cast<uint32_t>(gx + 1 >= 0 && gx + 1 < a.W) << 1))
+             << (2 * i);
+  }
+  uint32_t raw[kSlPer];
+  uint32_t inb = 0u;  // 2 bits per pair: element loaded (inside the raster)
+  auto load_chunk = [&](int k) {
+    inb = 0u;
+    const int64_t gy0 = ys - R + static_cast<int64_t>(k) * kSlCH;
+#pragma unroll
+    for (int i = 0; i < kSlPer; ++i) {
+      raw[i] = 0u;
+      if (prow[i] < 0) continue;
+      const int64_t gy = gy0 + prow[i];
+      if (gy < 0 || gy >= a.H) continue;
+      const uint32_t cb = (colin >> (2 * i)) & 3u;
+      const T* rp = src + gy * a.pitch + coff[i];
+      if (PAIR && cb == 3u) {
+        raw[i] = __ldg(reinterpret_cast<const uint32_t*>(rp));
+      } else {
+        const uint32_t e0 = (cb & 1u) ? static_cast<uint32_t>(static_cast<std::make_unsigned_t<T>>(__ldg(rp))) : 0u;
+        const uint32_t e1 = (cb & 2u) ? static_cast<uint32_t>(static_cast<std::make_unsigned_t<T>>(__ldg(rp + 1))) : 0u;
+        raw[i] = e0 | (e1 << 16);
+      }
+      inb |= cb << (2 * i);
+    }
+  };
+  auto store_chunk = [&](int slot) {
+#pragma unroll
+    for (int i = 0; i < kSlPer; ++i) {
+      if (prow[i] < 0) continue;
+      const int wc = (c + kSlTW * i) - prow[i] * (kSlSW / 2);
+      const uint32_t b = (inb >> (2 * i)) & 3u;
+      *reinterpret_cast<uint2*>(&ring[slot][prow[i]][2 * wc]) =
+          make_uint2(pack(raw[i] & 0xFFFFu, b & 1u), pack(raw[i] >> 16, (b >> 1) & 1u));
+    }
+  };
+
+  __shared__ float inv_n[Pk::kTaps + 1];  // correctly rounded 1/n for the float32 quotient
+  for (int i = c; i <= Pk::kTaps; i += kSlTW) inv_n[i] = i ? __frcp_rn(static_cast<float>(i)) : 0.0f;
+  load_chunk(0);
+  store_chunk(0);
+  __syncthreads();
+  if (nchunks > 1) load_chunk(1);
+  uint32_t h[2 * R + 1];
+#pragma unroll
+  for (int j = 0; j <= 2 * R; ++j) h[j] = 0u;
+  uint32_t V = 0u;
+  const int64_t x = x0 + c;
+  const bool col_in = x < a.W;
+  const bool f64 = a.out_dtype == VSR_F64;
+  // input row i (strip index); its output row is i - 2R (centre row i - R)
+  auto row_step = [&](int slot, int r, int i) {
+    const uint32_t* row = &ring[slot][r][c + kSlHalo - R];
+    uint32_t hn = 0u;
+#pragma unroll
+    for (int t = 0; t <= 2 * R; ++t) hn += row[t];
+    V += hn - h[0];
+#pragma unroll
+    for (int j = 0; j < 2 * R; ++j) h[j] = h[j + 1];
+    h[2 * R] = hn;
+    const int jc = i - R;
+    const uint32_t pc = ring[(jc >> 4) & 1][jc & (kSlCH - 1)][c + kSlHalo];
+    const int cnt = static_cast<int>(V >> Pk::kShift);
+    const int sum = static_cast<int>(V & kLow) - OFF * cnt;
+    if (i >= 2 * R && col_in) {
+      const int64_t o = (ys + (i - 2 * R)) * a.out_pitch + x;
+      const bool nd = pc == 0u || cnt == 0;
+      if (f64) {
+        static_cast<double*>(dst)[o] = nd ? a.nd_out : static_cast<double>(sum) / static_cast<double>(cnt);
+      } else {
+        // RN(sum / cnt): quotient with the exact reciprocal, one FMA correction
+        // (Markstein); sum and cnt are exact in float32
+        const float fs = static_cast<float>(sum), fn = static_cast<float>(cnt), rn = inv_n[cnt];
+        const float q0 = fs * rn;
+        const float q = fmaf(fmaf(-q0, fn, fs), rn, q0);
+        static_cast<float*>(dst)[o] = nd ? static_cast<float>(a.nd_out) : q;
+      }
+    }
+  };
+  for (int k = 0; k < nchunks; ++k) {
+    const int slot = k & 1;
+    if ((k + 1) * kSlCH <= nin) {
+#pragma unroll
+      for (int r = 0; r < kSlCH; ++r) row_step(slot, r, k * kSlCH + r);
+    } else {
+      for (int r = 0; k * kSlCH + r < nin; ++r) row_step(slot, r, k * kSlCH + r);
+    }
+    __syncthreads();  // every read of this chunk and of the last rows of the previous one is done
+    if (k + 1 < nchunks) {
+      store_chunk((k + 1) & 1);
+      __syncthreads();
+      if (k + 2 < nchunks) load_chunk(k + 2);
+    }
+  }
+}
+
+template <int R, typename T>
+int launch_slide_t(const BoxArgs& a, cudaStream_t st, int bands) {
+  const bool pair = sizeof(T) == 2 && aligned(a.src, 4) && a.pitch % 2 == 0 && a.band_stride % 2 == 0;
+  dim3 grid(static_cast<unsigned>((a.W + kSlTW - 1) / kSlTW), static_cast<unsigned>((a.H + kSlStrip - 1) / kSlStrip),
+            bands);
+  if (grid.y > 65535u) return fail(VSR_ERR_UNSUPPORTED, "raster too tall for the focal mean grid");
+  if (pair) box_slide_int<R, T, true><<<grid, kSlTW, 0, st>>>(a);
+  else box_slide_int<R, T, false><<<grid, kSlTW, 0, st>>>(a);
+  VSR_CUDA_TRY(cudaGetLastError());
+  return VSR_OK;
+}
+
+template <int R>
+int launch_slide_r(const BoxArgs& a, cudaStream_t st, int bands) {
+  switch (a.dtype) {
+    case VSR_U8: return launch_slide_t<R, uint8_t>(a, st, bands);
+    case VSR_I16: return launch_slide_t<R, int16_t>(a, st, bands);
+    default: return launch_slide_t<R, uint16_t>(a, st, bands);
+  }
+}
+
+// Square windows of radius 1..7 on 8/16-bit integer rasters; 0 otherwise.
+int launch_slide(const BoxArgs& a, cudaStream_t st, int bands) {
+  if (a.ry != a.rx) return -1;
+  switch (a.ry) {
+    case 1: return launch_slide_r<1>(a, st, bands);
+    case 2: return launch_slide_r<2>(a, st, bands);
+    case 3: return launch_slide_r<3>(a, st, bands);
+    case 4: return launch_slide_r<4>(a, st, bands);
+    case 5: return launch_slide_r<5>(a, st, bands);
+    case 6: return launch_slide_r<6>(a, st, bands);
+    case 7: return launch_slide_r<7>(a, st, bands);
+    default: return -1;
+  }
+}
+
 // ------------------------------------------------------- shared checks --
 int check_raster(const void* src, int dtype, int64_t H, int64_t W, int64_t pitch, const void* dst,
                  int out_dtype, int64_t out_pitch) {
@@ -1091,9 +1292,12 @@ static int focal_mean_impl(const void* src, int dtype, int bands, int64_t band_s
   switch (dtype) {
     case VSR_U8:
     case VSR_I16:
-    case VSR_U16:
+    case VSR_U16: {
+      const int rc2 = launch_slide(a, st, bands);  // square windows up to 15 x 15
+      if (rc2 >= 0) return rc2;
       // int32 sums stay exact for windows of <= 1023 16-bit values
       if ((2 * radius_y + 1) * (2 * radius_x + 1) <= kMaxFastWindow) return launch_box_fast<false>(a, st, bands);
+    }
       return launch_box<AccD>(a, st, bands);
     case VSR_F32:
       if ((2 * radius_y + 1) * (2 * radius_x + 1) <= kMaxFastWindow) return launch_box_fast<true>(a, st, bands);
