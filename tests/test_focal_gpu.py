@@ -176,3 +176,25 @@ def test_focal_mean_multiband_uint16_equals_per_band(vsr):
     allb = algebra.focal_mean_bands(r, 3, 3, out_dtype=np.float32).cpu().numpy()
     for i in range(3):
         np.testing.assert_array_equal(allb[i], oracle.focal_mean(stack[i], 3, 3, 0).astype(np.float32))
+
+
+@pytest.mark.parametrize("dtype,nodata", [(np.float32, -9999.0), (np.uint16, 0), (np.float32, float("nan"))])
+def test_large_gaussian_strip_segments(vsr, dtype, nodata):
+    """sigma 8, 65 x 65 on a raster taller than one 512-row segment and wider
+    than one 128-column strip (the ring and segment seams), float32 output."""
+    from vsr_gb300 import algebra
+
+    rng = np.random.default_rng(65)
+    shape = (1100, 300)
+    if dtype == np.uint16:
+        d = rng.integers(0, 10000, shape).astype(dtype)
+    else:
+        d = (rng.random(shape) * 5 + np.linspace(0, 100, shape[0] * shape[1]).reshape(shape)).astype(dtype)
+    d[rng.random(shape) < 0.02] = nodata
+    w = oracle.gaussian_weights(8.0, 65)
+    ref = oracle.convolve_normalized(d, w, nodata)
+    r = vsr.from_numpy(d, nodata=nodata)
+    out = vsr.raster_gaussian_filter(r, 8.0, kernel_size=65, precision="fp32").to_numpy()
+    _assert_close(out, ref, d, nodata)
+    out32 = algebra.gaussian_bands(r, 8.0, 65, precision="fp32", out_dtype=np.float32).cpu().numpy()[0]
+    _assert_close(out32.astype(np.float64), ref, d, nodata)

@@ -437,160 +437,189 @@ int launch_sep(const SepArgs& a, cudaStream_t st, int bands = 1) {
 constexpr int kMaxSepK = 33;
 
 // ------------------------------------------------------------ sep_strip --
-// Separable Gaussian for large k: a CTA walks a 128-column strip down a
-// segment of rows.  Each input row is reduced along x ONCE (row pass: weighted
-// sums of v*valid and of valid over the kernel width) into a ring of the last
-// k + kSBR - 1 row results in shared memory; every kSBR new rows the column
-// pass combines k ring rows into kSBR output rows.  Work per output pixel is
-// ~4k FMAs (plus k/kSSEG of row-pass halo) instead of 2k^2.
+// Separable Gaussian for large k (> 33, e.g. sigma 8 -> 65 x 65): a CTA walks
+// a 128-column strip down a 512-row segment.  Every input row is reduced
+// along x once (row pass) into a ring of the last k + 15 row results; every
+// 16 new rows the column pass combines k ring rows into 16 output rows.
+// Numerator (v * valid) and weight sum (valid) travel together as float2
+// pairs through Blackwell's packed FP32 FMA (fma.rn.f32x2), so both sums cost
+// one instruction per tap.  Each lane makes 8 adjacent outputs per pass from
+// a register window of 15 values advanced 8 taps at a time, the tap weight a
+// shared-memory broadcast.  Work per output pixel: 2k packed FMAs.
 constexpr int kSTW2 = 128;  // strip width
-constexpr int kSBR = 8;     // rows per step
+constexpr int kSBR = 16;    // rows per step
 constexpr int kSSEG = 512;  // rows per CTA segment
+
+__host__ __device__ inline int strip_pos(int i) { return i + (i >> 3); }  // conflict-free 8-wide lane strides
+__host__ __device__ inline int strip_pw(int k) { return strip_pos(kSTW2 + k + 7) + 1; }
 
 inline size_t strip_smem_bytes(int k) {
   const int NR = k + kSBR - 1;
-  const int SW = kSTW2 + k - 1;
-  return static_cast<size_t>(2 * NR * kSTW2 + 2 * kSBR * padded_width(SW) + ((k + 3) & ~3)) * 4 + 16;
+  const int k8 = (k + 7) & ~7;
+  return (static_cast<size_t>(NR) * kSTW2 + static_cast<size_t>(kSBR) * strip_pw(k) + k8) * sizeof(float2) + 16;
 }
 
-__global__ void __launch_bounds__(256) sep_strip(const SepArgs a) {
-  extern __shared__ __align__(16) float ssm[];
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+// One staged tap: (v * valid, valid); out-of-raster taps are (0, 0).  DT is
+// the raster's dtype when known at compile time (0: dispatch at run time).
+template <int DT>
+__device__ __forceinline__ float2 strip_tap(const void* src, int dtype, int64_t idx, const NodataSpec& nd) {
+  bool ok;
+  float x;
+  if (DT == VSR_U16) {
+    const int v = __ldg(static_cast<const uint16_t*>(src) + idx);
+    ok = !(nd.kind == VSR_NODATA_VALUE && v == nd.iv);
+    x = static_cast<float>(v);
+  } else if (DT == VSR_F32) {
+    x = __ldg(static_cast<const float*>(src) + idx);
+    ok = !(nd.kind == VSR_NODATA_VALUE ? x == nd.fv : (nd.kind == VSR_NODATA_NAN ? x != x : false));
+  } else {
+    x = load_elem(src, dtype, idx, nd, ok);
+  }
+  return make_float2(x * (ok ? 1.0f : 0.0f), ok ? 1.0f : 0.0f);  // NaN * 0 stays NaN (reference poisoning)
+}
+
+template <int DT>
+__global__ void __launch_bounds__(256, 2) sep_strip(const SepArgs a) {
+  extern __shared__ __align__(16) float2 ssm2[];
   const int k = a.k, r = k / 2;
   const int NR = k + kSBR - 1;
-  const int SW = kSTW2 + k - 1, PW = padded_width(SW);
-  float* Rn = ssm;                 // NR x kSTW2 ring (numerator)
-  float* Rd = Rn + NR * kSTW2;     // NR x kSTW2 ring (weight sum)
-  float* vz = Rd + NR * kSTW2;     // kSBR x PW staged v*valid
-  float* vd = vz + kSBR * PW;      // kSBR x PW staged valid
-  float* g = vd + kSBR * PW;
+  const int PW = strip_pw(k);
+  const int k8 = (k + 7) & ~7;
+  float2* ring = ssm2;                  // NR x 128 (num, den) row-pass results
+  float2* stg = ring + NR * kSTW2;      // kSBR x PW staged (v * valid, valid)
+  float2* g2 = stg + kSBR * PW;         // k8 weight pairs (w, w), zero padded
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t x0 = static_cast<int64_t>(blockIdx.x) * kSTW2;
   const int64_t ys = static_cast<int64_t>(blockIdx.y) * kSSEG;
   const int64_t ye = min(ys + kSSEG, a.H);
   const void* src = band_src(a.src, a.dtype, a.band_stride);
   void* dst = band_dst(a.dst, a.out_dtype, a.out_band_stride);
-  for (int i = tid; i < ((k + 3) & ~3); i += 256) g[i] = a.g32[i];  // zero padded by the prep kernel
-
+  for (int i = tid; i < k8; i += 256) {
+    const float w = i < k ? a.g32[i] : 0.0f;
+    g2[i] = make_float2(w, w);
+  }
+  const int SW = kSTW2 + k - 1;  // staged columns x0 - r .. x0 + 127 + r
   // Input rows ys - r .. ye + r - 1 pass through the ring; row gy lives in
   // slot (gy - (ys - r)) % NR.
   const int64_t first = ys - r;
   const int64_t last = ye + r;  // exclusive
   int64_t next_out = ys;
-  for (int64_t rb = first; rb < last; rb += kSBR) {
-    __syncthreads();  // previous column pass is done with the staging rows
-    // stage kSBR input rows (or fewer at the end): warp q takes row q
-    {
-      const int q = warp;
+  // staging: thread tid takes columns tid, tid + 256 of each of the kSBR
+  // rows; the next step's taps are loaded into registers during this
+  // step's passes
+  constexpr int kCols = 1;  // SW <= 128 + 79 < 256 threads
+  float2 pre[kSBR][kCols];
+  auto load_step = [&](int64_t rb) {
+#pragma unroll
+    for (int q = 0; q < kSBR; ++q) {
       const int64_t gy = rb + q;
       const bool row_in = gy < last && gy >= 0 && gy < a.H;
-      for (int c = lane; c < SW; c += 32) {
+#pragma unroll
+      for (int j = 0; j < kCols; ++j) {
+        const int c = tid + 256 * j;
         const int64_t gx = x0 + c - r;
-        float v = 0.0f, d = 0.0f;
-        if (row_in && gx >= 0 && gx < a.W) {
-          bool ok;
-          const float x = load_elem(src, a.dtype, gy * a.pitch + gx, a.nd, ok);
-          v = x * (ok ? 1.0f : 0.0f);  // NaN * 0 stays NaN, as in the reference
-          d = ok ? 1.0f : 0.0f;
-        }
-        vz[q * PW + pos(c)] = v;
-        vd[q * PW + pos(c)] = d;
+        pre[q][j] = (row_in && c < SW && gx >= 0 && gx < a.W) ? strip_tap<DT>(src, a.dtype, gy * a.pitch + gx, a.nd)
+                                                              : make_float2(0.0f, 0.0f);
       }
     }
+  };
+  load_step(first);
+  for (int64_t rb = first; rb < last; rb += kSBR) {
+    __syncthreads();  // the previous step's passes are done with the staging rows and ring slots
+#pragma unroll
+    for (int q = 0; q < kSBR; ++q)
+#pragma unroll
+      for (int j = 0; j < kCols; ++j) {
+        const int c = tid + 256 * j;
+        if (c < SW) stg[q * PW + strip_pos(c)] = pre[q][j];
+      }
     __syncthreads();
-    // row pass: warp q handles staged row q, 4 columns per lane; taps are
-    // walked 4 at a time over a 7-value window (no large register arrays)
+    if (rb + kSBR < last) load_step(rb + kSBR);
+    // row pass: half-warp h takes staged row 2 warp + h, 8 columns per lane
     {
-      const int q = warp;
+      const int q = 2 * warp + (lane >> 4);
       const int64_t gy = rb + q;
       if (gy < last) {
         const int slot = static_cast<int>((gy - first) % NR);
-        const int c0 = 4 * lane;
+        const int c0 = 8 * (lane & 15);
+        const float2* row = stg + q * PW;
+        float2 acc[8];
 #pragma unroll
-        for (int plane = 0; plane < 2; ++plane) {
-          const float* row = (plane == 0 ? vz : vd) + q * PW;
-          float acc[4] = {};
-          float a0 = row[pos(c0)], a1 = row[pos(c0 + 1)], a2 = row[pos(c0 + 2)];
-          for (int t = 0; t < k; t += 4) {
-            // columns past the staged row are read (inside the buffer) but
-            // never multiplied: taps t+j >= k are skipped
-            const float b0 = row[pos(c0 + t + 3)], b1 = row[pos(c0 + t + 4)];
-            const float b2 = row[pos(c0 + t + 5)], b3 = row[pos(c0 + t + 6)];
-            const float V[7] = {a0, a1, a2, b0, b1, b2, b3};
+        for (int u = 0; u < 8; ++u) acc[u] = make_float2(0.0f, 0.0f);
+        float2 win[15];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-              if (t + j < k) {
-                const float w = g[t + j];
+        for (int j = 0; j < 7; ++j) win[j] = row[strip_pos(c0 + j)];
+        for (int t = 0; t < k; t += 8) {
 #pragma unroll
-                for (int u = 0; u < 4; ++u) acc[u] = fmaf(w, V[u + j], acc[u]);
-              }
+          for (int j = 0; j < 8; ++j) win[7 + j] = row[strip_pos(c0 + t + 7 + j)];  // inside the padded row
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            if (t + j < k) {  // taps past k are never multiplied (their values may be NaN)
+              const float2 w = g2[t + j];
+#pragma unroll
+              for (int u = 0; u < 8; ++u) acc[u] = ffma2(w, win[u + j], acc[u]);
             }
-            a0 = b1;
-            a1 = b2;
-            a2 = b3;
           }
-          *reinterpret_cast<float4*>((plane == 0 ? Rn : Rd) + slot * kSTW2 + c0) =
-              make_float4(acc[0], acc[1], acc[2], acc[3]);
+#pragma unroll
+          for (int j = 0; j < 7; ++j) win[j] = win[8 + j];
         }
+        float2* dst_ring = ring + slot * kSTW2 + c0;
+#pragma unroll
+        for (int u = 0; u < 8; u += 2)
+          *reinterpret_cast<float4*>(dst_ring + u) = make_float4(acc[u].x, acc[u].y, acc[u + 1].x, acc[u + 1].y);
       }
     }
     __syncthreads();
-    // column pass for the output rows whose window [y-r, y+r] is now in the
-    // ring (at most kSBR per step): 2 groups of 128 threads, 4 rows each,
-    // taps walked 4 at a time over a 7-row window of the ring
+    // column pass for the output rows whose window [y - r, y + r] is now in
+    // the ring (at most kSBR per step): 2 groups of 128 threads, 8 rows each
     const int64_t ready_to = min(rb + kSBR - r, ye);  // outputs y < ready_to are complete
     if (ready_to > next_out) {
       const int c = tid & (kSTW2 - 1);
       const int grp = tid >> 7;
       const int64_t x = x0 + c;
-      const int64_t yb = next_out + 4 * grp;
+      const int64_t yb = next_out + 8 * grp;
       if (yb < ready_to) {
-        float num[4] = {}, den[4] = {};
+        float2 acc[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) acc[u] = make_float2(0.0f, 0.0f);
         int sl = static_cast<int>((yb - r - first) % NR);
         auto nxt = [&](int v) { return v + 1 == NR ? 0 : v + 1; };
-        float an[3], ad[3];
+        float2 win[15];
 #pragma unroll
-        for (int m = 0; m < 3; ++m) {
-          an[m] = Rn[sl * kSTW2 + c];
-          ad[m] = Rd[sl * kSTW2 + c];
+        for (int j = 0; j < 7; ++j) {
+          win[j] = ring[sl * kSTW2 + c];
           sl = nxt(sl);
         }
-        for (int t = 0; t < k; t += 4) {
-          float bn[4], bd[4];
+        for (int t = 0; t < k; t += 8) {
 #pragma unroll
-          for (int m = 0; m < 4; ++m) {
-            // ring slots past the window hold other rows: read, never used
-            bn[m] = Rn[sl * kSTW2 + c];
-            bd[m] = Rd[sl * kSTW2 + c];
+          for (int j = 0; j < 8; ++j) {
+            win[7 + j] = ring[sl * kSTW2 + c];  // slots past the window hold other rows: read, never used
             sl = nxt(sl);
           }
-          const float Vn[7] = {an[0], an[1], an[2], bn[0], bn[1], bn[2], bn[3]};
-          const float Vd[7] = {ad[0], ad[1], ad[2], bd[0], bd[1], bd[2], bd[3]};
 #pragma unroll
-          for (int j = 0; j < 4; ++j) {
+          for (int j = 0; j < 8; ++j) {
             if (t + j < k) {
-              const float w = g[t + j];
+              const float2 w = g2[t + j];
 #pragma unroll
-              for (int u = 0; u < 4; ++u) {
-                num[u] = fmaf(w, Vn[u + j], num[u]);
-                den[u] = fmaf(w, Vd[u + j], den[u]);
-              }
+              for (int u = 0; u < 8; ++u) acc[u] = ffma2(w, win[u + j], acc[u]);
             }
           }
 #pragma unroll
-          for (int m = 0; m < 3; ++m) {
-            an[m] = bn[m + 1];
-            ad[m] = bd[m + 1];
-          }
+          for (int j = 0; j < 7; ++j) win[j] = win[8 + j];
         }
         if (x < a.W) {
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
+          for (int u = 0; u < 8; ++u) {
             const int64_t y = yb + u;
             if (y >= ready_to) break;
-            bool centre_ok;
-            (void)load_elem(src, a.dtype, y * a.pitch + x, a.nd, centre_ok);
-            const double out = (centre_ok && den[u] > 0.0f) ? static_cast<double>(num[u] / den[u]) : a.nd_out;
-            store_out(dst, a.out_dtype, y * a.out_pitch + x, out);
+            // centre validity: its staged weight is 1 (in the raster and not nodata)
+            const bool centre_ok = strip_tap<DT>(src, a.dtype, y * a.pitch + x, a.nd).y != 0.0f;
+            const float num = acc[u].x, den = acc[u].y;
+            const bool ok = centre_ok && den > 0.0f;
+            if (a.out_dtype == VSR_F64) static_cast<double*>(dst)[y * a.out_pitch + x] = ok ? static_cast<double>(num / den) : a.nd_out;
+            else static_cast<float*>(dst)[y * a.out_pitch + x] = ok ? num / den : static_cast<float>(a.nd_out);
           }
         }
       }
@@ -601,9 +630,11 @@ __global__ void __launch_bounds__(256) sep_strip(const SepArgs a) {
 
 int launch_strip(const SepArgs& a, cudaStream_t st, int bands) {
   const size_t smem = strip_smem_bytes(a.k);
-  auto kern = sep_strip;
+  if (smem > 227 * 1024) return fail(VSR_ERR_UNSUPPORTED, "Gaussian kernel %d too large for the strip kernel", a.k);
+  auto kern = a.dtype == VSR_U16 ? sep_strip<VSR_U16> : (a.dtype == VSR_F32 ? sep_strip<VSR_F32> : sep_strip<0>);
   VSR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   dim3 grid(static_cast<unsigned>((a.W + kSTW2 - 1) / kSTW2), static_cast<unsigned>((a.H + kSSEG - 1) / kSSEG), bands);
+  if (grid.y > 65535u) return fail(VSR_ERR_UNSUPPORTED, "raster too tall for the Gaussian grid");
   kern<<<grid, 256, smem, st>>>(a);
   VSR_CUDA_TRY(cudaGetLastError());
   return VSR_OK;
