@@ -268,10 +268,14 @@ def run_vsr(args, ws, rank, local):
         peak, peak_kind = _roofline_peak()
         lmed = statistics.mean(launch_ms)
         achieved = BYTES_PER_PX * px / (lmed * 1e-3) / 1e9
-        traffic_file = ROOT / "profiles" / "horn_f32_tma_terrain16k_traffic.json"
+        # dram read + write bytes per launch from the ncu capture summarised in
+        # profiles/ (8192^2 capture scaled to 16384^2 by pixel count)
         traffic = None
-        if traffic_file.exists():
-            traffic = json.loads(traffic_file.read_text()).get("bytes_per_launch")
+        summary = ROOT / "profiles" / "horn_f32_tma_terrain8k_ncu.md"
+        if summary.exists() and H == 16384:
+            for line in summary.read_text().splitlines():
+                if line.strip().startswith("traffic_bytes_per_launch_16384"):
+                    traffic = int(line.split("=")[1])
         # CPU baseline: the oracle, single thread, on a bounded row sample.
         host = in_np
         cpu_rows = 512

@@ -85,7 +85,8 @@ VSR_API int vsr_poll_device_error(void* stream, uint32_t* code);
 
 /* ---- launch-configuration tuning ----------------------------------------
  * Tunable operations have a small table of launch configurations (tile
- * shape, halo staging depth, threads per CTA).  The autotuner
+ * shape, halo staging depth, threads per CTA, output staging, register
+ * budget).  The autotuner
  * (vsr_gb300.autotune) times them on the caller's own data and stores the
  * winner with vsr_tuning_set; the choice is process-wide.  No counterpart in
  * the reference, whose launches use one fixed 16 x 16 block

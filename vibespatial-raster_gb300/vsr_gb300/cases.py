@@ -1,0 +1,95 @@
+"""Single-operation timing cases on synthetic device rasters.
+
+``python -m vsr_gb300.cases <op> [options]`` builds one seeded synthetic
+input on ``cuda:0`` (the shapes and value distributions of the benchmark
+workloads), runs the operation through the public API a few times to warm
+up, then times ``--reps`` calls with CUDA events and prints one JSON line.
+It is the small, single-kernel command to run under a profiler:
+
+    conv        trend-plus-noise float32 raster, seeded normalised k x k weights
+                (the 8192^2 convolution workload at a chosen size)
+    focal_mean  uint16 band stack, gamma-like values 0..9999, 3 % nodata 0
+                (the 12 x 10980^2 multiband workload, fewer bands)
+    gaussian    the same uint16 stack, Gaussian sigma / kernel size
+
+Run with ``PYTHONPATH=vibespatial-raster_gb300`` from the repository root.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+
+import numpy as np
+
+
+def _timed(fn, reps: int) -> float:
+    import torch
+
+    for _ in range(3):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        fn()
+    b.record()
+    b.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def _uint16_stack(bands: int, size: int):
+    import torch
+
+    dev = torch.device("cuda", 0)
+    g = torch.Generator(device=dev).manual_seed(4)
+    x = torch.randint(1, 10000, (bands, size, size), generator=g, device=dev, dtype=torch.int32)
+    hole = torch.rand((bands, size, size), generator=g, device=dev) < 0.03
+    x[hole] = 0
+    return x.to(torch.uint16)
+
+
+def main(argv=None) -> None:
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("op", choices=["conv", "focal_mean", "gaussian"])
+    ap.add_argument("--size", type=int, default=None, help="raster side (default: 4096 conv, 10980 others)")
+    ap.add_argument("--bands", type=int, default=1)
+    ap.add_argument("--k", type=int, default=31, help="kernel side (conv, gaussian)")
+    ap.add_argument("--sigma", type=float, default=8.0)
+    ap.add_argument("--radius", type=int, default=3)
+    ap.add_argument("--precision", default="split_bf16", choices=["auto", "fp32", "split_bf16"])
+    ap.add_argument("--reps", type=int, default=5)
+    args = ap.parse_args(argv)
+
+    import torch
+
+    import vsr_gb300 as vsr
+    from vsr_gb300 import algebra, workloads
+
+    vsr.load_library()
+    dev = torch.device("cuda", 0)
+    if args.op == "conv":
+        n = args.size or 4096
+        r = vsr.from_device(workloads.trend_noise(n, n, device=dev))
+        w = workloads.random_weights(args.k, 200 + args.k)
+        out = torch.empty((1, n, n), dtype=torch.float32, device=dev)
+        ms = _timed(lambda: algebra.convolve_bands(r, w, precision=args.precision, out_dtype=np.float32, out=out),
+                    args.reps)
+        px = n * n
+    else:
+        n = args.size or 10980
+        r = vsr.from_device(_uint16_stack(args.bands, n), nodata=0)
+        out = torch.empty((args.bands, n, n), dtype=torch.float32, device=dev)
+        if args.op == "focal_mean":
+            fn = lambda: algebra.focal_mean_bands(r, args.radius, args.radius, out_dtype=np.float32, out=out)  # noqa: E731
+        else:
+            fn = lambda: algebra.gaussian_bands(r, args.sigma, args.k, precision="auto", out_dtype=np.float32,  # noqa: E731
+                                                out=out)
+        ms = _timed(fn, args.reps)
+        px = args.bands * n * n
+    print(json.dumps({"op": args.op, "size": n, "bands": args.bands, "ms": ms, "gpix_s": px / ms / 1e6,
+                      "options": {k: v for k, v in vars(args).items() if k not in ("op", "size", "bands")}}))
+
+
+if __name__ == "__main__":
+    main()
