@@ -924,8 +924,18 @@ template <int TH, int THREADS, int KG>
 struct BatchSmem {
   static constexpr int HY = KG / 2 > 0 ? KG / 2 : 1;  // staged halo rows (>= 1 for Horn)
   static constexpr int SR = TH + 2 * HY;              // staged rows
-  static constexpr int kFloats = SR * kSW + 2 * SR * kTW;
+  static constexpr int kFloats = 2 * SR * kSW + 2 * SR * kTW;  // two staging buffers, row-pass sums
 };
+
+// 4-byte asynchronous global -> shared copy (any alignment of the source row).
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
 
 constexpr int kBatchSmemTiles = 2048;  // tiles whose prefix sums are searched in shared memory
 
@@ -938,88 +948,112 @@ __global__ void __launch_bounds__(THREADS) batch_terrain_kernel(BatchHeader* __r
   constexpr int HY = L::HY, SR = L::SR;
   static_assert(RB * WARPS == TH && RB % 2 == 0, "rows per warp");
   extern __shared__ __align__(16) float bsm[];
-  float* S = bsm;                 // SR x kSW staged values
-  float* Rn = S + SR * kSW;       // SR x kTW row-pass numerator
-  float* Rd = Rn + SR * kTW;      // SR x kTW row-pass weight sum
+  float* Sbuf = bsm;                  // 2 x SR x kSW staged values (double buffered)
+  float* Rn = Sbuf + 2 * SR * kSW;    // SR x kTW row-pass numerator
+  float* Rd = Rn + SR * kTW;          // SR x kTW row-pass weight sum
   __shared__ int64_t sh_first[kBatchSmemTiles];
-  __shared__ int64_t sh_item;
-  __shared__ int sh_tile;
-  __shared__ HornParams sh_P;
-  __shared__ float sh_nd;
+  __shared__ int64_t sh_item[2];
+  __shared__ int sh_tile[2];
+  __shared__ HornParams sh_P[2];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t total = hdr->total_items;
   const int n_tiles = hdr->n_tiles;
   const bool smem_search = n_tiles <= kBatchSmemTiles;
   if (smem_search)
     for (int i = tid; i < n_tiles; i += THREADS) sh_first[i] = tiles[i].first_item;
-  int cur_tile = -1;
-  // the next item is claimed one step ahead, so the atomic's latency overlaps
-  // the current item's work
-  int64_t next_item = 0;
-  if (tid == 0) next_item = static_cast<int64_t>(atomicAdd(&hdr->counter, 1ull));
+  float gw[KG > 0 ? KG : 1];
+#pragma unroll
+  for (int t = 0; t < KG; ++t) gw[t] = hdr->g[t];
+  const float gs2 = hdr->gsum * hdr->gsum;
   __syncthreads();
 
-  for (;;) {
-    if (tid == 0) {
-      const int64_t item = next_item;
-      sh_item = item;
-      if (item < total) {
-        next_item = static_cast<int64_t>(atomicAdd(&hdr->counter, 1ull));
-        int lo = 0, hi = n_tiles - 1;  // last tile with first_item <= item
-        while (lo < hi) {
-          const int mid = (lo + hi + 1) >> 1;
-          const int64_t f = smem_search ? sh_first[mid] : tiles[mid].first_item;
-          if (f <= item) lo = mid;
-          else hi = mid - 1;
-        }
-        sh_tile = lo;
-        if (lo != cur_tile) {  // consecutive items usually share a tile
-          cur_tile = lo;
-          const BatchTileDev& T = tiles[lo];
-          HornParams P{};
-          P.height = T.H;
-          P.width = T.W;
-          P.in_pitch = T.pitch;
-          P.out_pitch = T.out_pitch;
-          P.hs_pitch = T.out_pitch;
-          P.inv8cx = T.inv8cx;
-          P.inv8cy = T.inv8cy;
-          P.nd_out_f = static_cast<float>(T.nodata);
-          P.nd_out_d = T.nodata;
-          P.flags = T.flags;
-          P.nd_kind = T.nd_kind;
-          sh_P = P;
-          sh_nd = static_cast<float>(T.nodata);
-        }
+  // Items are claimed from the atomic counter one ahead of the one being
+  // staged, and staged (cp.async into the other buffer) one ahead of the one
+  // being computed, so claim and copy latencies overlap the current item.
+  int64_t claimed = 0;  // (thread 0) the next unassigned claim
+  auto assign = [&](int b, int64_t item) {  // thread 0: item -> buffer b's tile and params
+    sh_item[b] = item;
+    if (item >= total) return;
+    int lo = 0, hi = n_tiles - 1;  // last tile with first_item <= item
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      const int64_t f = smem_search ? sh_first[mid] : tiles[mid].first_item;
+      if (f <= item) lo = mid;
+      else hi = mid - 1;
+    }
+    sh_tile[b] = lo;
+    const BatchTileDev& T = tiles[lo];
+    HornParams P{};
+    P.height = T.H;
+    P.width = T.W;
+    P.in_pitch = T.pitch;
+    P.out_pitch = T.out_pitch;
+    P.hs_pitch = T.out_pitch;
+    P.inv8cx = T.inv8cx;
+    P.inv8cy = T.inv8cy;
+    P.nd_out_f = static_cast<float>(T.nodata);
+    P.nd_out_d = T.nodata;
+    P.flags = T.flags;
+    P.nd_kind = T.nd_kind;
+    sh_P[b] = P;
+  };
+  // Stage rows y0-HY .. y0+TH+HY-1, columns x0-4 .. x0+131 (clamped into the
+  // tile: edge replication), one warp per row, lanes along the row.
+  auto stage = [&](int b) {
+    const int64_t item = sh_item[b];
+    if (item >= total) return;
+    const HornParams& P = sh_P[b];
+    const BatchTileDev& T = tiles[sh_tile[b]];
+    const int64_t local = item - (smem_search ? sh_first[sh_tile[b]] : T.first_item);
+    const int64_t items_x = (P.width + kTW - 1) / kTW;
+    const int64_t by = local / items_x, bx = local - by * items_x;
+    const int64_t x0 = bx * kTW, y0 = by * TH;
+    float* S = Sbuf + b * SR * kSW;
+    for (int r = warp; r < SR; r += WARPS) {
+      const int64_t gy = min(max(y0 - HY + r, int64_t(0)), P.height - 1);
+      const float* rowp = T.src + gy * P.in_pitch;
+#pragma unroll
+      for (int c = lane; c < kSW; c += 32) {
+        const int64_t gx = min(max(x0 - 4 + c, int64_t(0)), P.width - 1);
+        cp_async4(S + r * kSW + c, rowp + gx);
       }
     }
+  };
+  if (tid == 0) {
+    assign(0, static_cast<int64_t>(atomicAdd(&hdr->counter, 1ull)));
+    claimed = static_cast<int64_t>(atomicAdd(&hdr->counter, 1ull));
+  }
+  __syncthreads();
+  stage(0);
+  cp_async_commit();
+
+  for (int it = 0;; ++it) {
+    const int b = it & 1;
+    if (sh_item[b] >= total) break;  // uniform: written before the last barrier
+    if (tid == 0) {
+      assign(b ^ 1, claimed);
+      if (claimed < total) claimed = static_cast<int64_t>(atomicAdd(&hdr->counter, 1ull));
+    }
+    __syncthreads();  // buffer b ^ 1's item is known (and its previous reads are done)
+    stage(b ^ 1);
+    cp_async_commit();
+    cp_async_wait<1>();  // this item's copies (all but the group just committed)
     __syncthreads();
-    const int64_t item = sh_item;
-    if (item >= total) break;
-    const BatchTileDev& T = tiles[sh_tile];
-    const HornParams P = sh_P;
-    const float nd_in = sh_nd;
-    const int64_t local = item - (smem_search ? sh_first[sh_tile] : T.first_item);
+    const int64_t item = sh_item[b];
+    const BatchTileDev& T = tiles[sh_tile[b]];
+    const HornParams P = sh_P[b];
+    const float nd_in = static_cast<float>(P.nd_out_d);
+    const int64_t local = item - (smem_search ? sh_first[sh_tile[b]] : T.first_item);
     const int64_t items_x = (P.width + kTW - 1) / kTW;
     const int64_t by = local / items_x, bx = local - by * items_x;
     const int64_t x0 = bx * kTW, y0 = by * TH;
     const int64_t H = P.height, W = P.width;
-    const float* srcp = T.src;
+    const float* S = Sbuf + b * SR * kSW;
 
-    // Stage rows y0-HY .. y0+TH+HY-1, columns x0-4 .. x0+131 (clamped), one
-    // warp per row, lanes along the row (coalesced for any pitch).
+    // Does the staged block hold nodata?  Clean blocks skip the mask logic.
     bool any_nd = false;
-    for (int r = warp; r < SR; r += WARPS) {
-      const int64_t gy = min(max(y0 - HY + r, int64_t(0)), H - 1);
-      const float* rowp = srcp + gy * P.in_pitch;
-#pragma unroll
-      for (int c = lane; c < kSW; c += 32) {
-        const int64_t gx = min(max(x0 - 4 + c, int64_t(0)), W - 1);
-        const float v = __ldg(rowp + gx);
-        S[r * kSW + c] = v;
-        any_nd |= is_nd(v, P.nd_kind, nd_in);
-      }
-    }
+    if (P.nd_kind != VSR_NODATA_NONE)
+      for (int i = tid; i < SR * kSW; i += THREADS) any_nd |= is_nd(S[i], P.nd_kind, nd_in);
     const bool masked = __syncthreads_or(any_nd);
     const bool edge = x0 + kTW > W || y0 + TH > H;
     const MaskRule rule = mask_rule(P);
@@ -1066,7 +1100,7 @@ __global__ void __launch_bounds__(THREADS) batch_terrain_kernel(BatchHeader* __r
         float an[4] = {}, ad[4] = {};
 #pragma unroll
         for (int t = 0; t < KG; ++t) {
-          const float w = hdr->g[t];
+          const float w = gw[t];
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
             an[u] = fmaf(w, z[u + t], an[u]);
@@ -1083,7 +1117,6 @@ __global__ void __launch_bounds__(THREADS) batch_terrain_kernel(BatchHeader* __r
       const int c = tid % kTW;
       const int q0 = (tid / kTW) * RY;
       const int64_t x = x0 + c;
-      const float gs2 = hdr->gsum * hdr->gsum;
 #pragma unroll 1
       for (int q = q0; q < q0 + RY; ++q) {
         const int64_t y = y0 + q;
@@ -1092,7 +1125,7 @@ __global__ void __launch_bounds__(THREADS) batch_terrain_kernel(BatchHeader* __r
 #pragma unroll
         for (int t = 0; t < KG; ++t) {
           const int r = q + HY - R + t;
-          const float w = hdr->g[t];
+          const float w = gw[t];
           num = fmaf(w, Rn[r * kTW + c], num);
           den = fmaf(w, Rd[r * kTW + c], den);
         }
@@ -1102,8 +1135,9 @@ __global__ void __launch_bounds__(THREADS) batch_terrain_kernel(BatchHeader* __r
         T.smooth[y * T.out_pitch + x] = (centre_ok && den > 0.0f) ? num / den : P.nd_out_f;
       }
     }
-    __syncthreads();  // staged block and row pass are reused by the next item
+    __syncthreads();  // row-pass sums are reused by the next item; buffer b is refilled after the next barrier
   }
+  cp_async_wait<0>();  // no copy may land after the CTA leaves
 }
 
 // Launch configurations the autotuner chooses between: (rows per block,
