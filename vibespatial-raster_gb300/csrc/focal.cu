@@ -456,10 +456,65 @@ __host__ __device__ inline int strip_pw(int k) { return strip_pos(kSTW2 + k + 7)
 inline size_t strip_smem_bytes(int k) {
   const int NR = k + kSBR - 1;
   const int k8 = (k + 7) & ~7;
-  return (static_cast<size_t>(NR) * kSTW2 + static_cast<size_t>(kSBR) * strip_pw(k) + k8) * sizeof(float2) + 16;
+  return (static_cast<size_t>(NR) * kSTW2 + static_cast<size_t>(kSBR) * strip_pw(k) + k8) * sizeof(float2) +
+         static_cast<size_t>(NR) * 8 * 4 + 16;  // + validity bits of 256 staged columns per ring row
 }
 
-__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+// acc[u] += sum_{t < k} g2[t] * fetch(u + t) for u = 0..7: 8 outputs from a
+// 15-value register window advanced 8 taps at a time.  KB > 0: k lies in
+// (8 (KB - 1), 8 KB] and the blocks are unrolled (the window shift becomes
+// register renaming, only the last block's taps are tested against k);
+// KB == 0: run-time k, full blocks unguarded, then the remainder.  Taps past
+// k are never multiplied: their window values may be NaN.
+template <int KB, class Fetch>
+__device__ __forceinline__ void taps8(const float2* __restrict__ g2, int k, Fetch fetch, float2 acc[8]) {
+  float2 win[15];
+#pragma unroll
+  for (int j = 0; j < 7; ++j) win[j] = fetch(j);
+  if (KB > 0) {
+#pragma unroll
+    for (int b = 0; b < KB; ++b) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) win[7 + j] = fetch(8 * b + 7 + j);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        if (b < KB - 1 || 8 * b + j < k) {
+          const float2 w = g2[8 * b + j];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) acc[u] = __ffma2_rn(w, win[u + j], acc[u]);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 7; ++j) win[j] = win[8 + j];
+    }
+  } else {
+    int t = 0;
+    for (; t + 8 <= k; t += 8) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) win[7 + j] = fetch(t + 7 + j);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const float2 w = g2[t + j];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) acc[u] = __ffma2_rn(w, win[u + j], acc[u]);
+      }
+#pragma unroll
+      for (int j = 0; j < 7; ++j) win[j] = win[8 + j];
+    }
+    if (t < k) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) win[7 + j] = fetch(t + 7 + j);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        if (t + j < k) {
+          const float2 w = g2[t + j];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) acc[u] = __ffma2_rn(w, win[u + j], acc[u]);
+        }
+      }
+    }
+  }
+}
 
 // One staged tap: (v * valid, valid); out-of-raster taps are (0, 0).  DT is
 // the raster's dtype when known at compile time (0: dispatch at run time).
@@ -480,7 +535,7 @@ __device__ __forceinline__ float2 strip_tap(const void* src, int dtype, int64_t 
   return make_float2(x * (ok ? 1.0f : 0.0f), ok ? 1.0f : 0.0f);  // NaN * 0 stays NaN (reference poisoning)
 }
 
-template <int DT>
+template <int DT, int KB>
 __global__ void __launch_bounds__(256, 2) sep_strip(const SepArgs a) {
   extern __shared__ __align__(16) float2 ssm2[];
   const int k = a.k, r = k / 2;
@@ -490,6 +545,7 @@ __global__ void __launch_bounds__(256, 2) sep_strip(const SepArgs a) {
   float2* ring = ssm2;                  // NR x 128 (num, den) row-pass results
   float2* stg = ring + NR * kSTW2;      // kSBR x PW staged (v * valid, valid)
   float2* g2 = stg + kSBR * PW;         // k8 weight pairs (w, w), zero padded
+  uint32_t* vbits = reinterpret_cast<uint32_t*>(g2 + k8);  // NR x 8 words: staged-column validity bits
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t x0 = static_cast<int64_t>(blockIdx.x) * kSTW2;
   const int64_t ys = static_cast<int64_t>(blockIdx.y) * kSSEG;
@@ -526,14 +582,24 @@ __global__ void __launch_bounds__(256, 2) sep_strip(const SepArgs a) {
     }
   };
   load_step(first);
-  for (int64_t rb = first; rb < last; rb += kSBR) {
-    __syncthreads();  // the previous step's passes are done with the staging rows and ring slots
+  __syncthreads();  // weights
+  int slot_rb = 0;  // ring slot of row rb: (rb - first) % NR, kept incrementally
+  for (int64_t rb = first; rb < last; rb += kSBR, slot_rb = (slot_rb + kSBR) % NR) {
+    // No barrier needed here: the staging rows were last read by the previous
+    // row pass (before its column pass); the barrier below keeps this step's
+    // row pass from overwriting ring rows the previous column pass reads.
 #pragma unroll
     for (int q = 0; q < kSBR; ++q)
 #pragma unroll
       for (int j = 0; j < kCols; ++j) {
         const int c = tid + 256 * j;
         if (c < SW) stg[q * PW + strip_pos(c)] = pre[q][j];
+        // validity of staged column c (the column pass reads its centres' bits)
+        const uint32_t bits = __ballot_sync(0xffffffffu, c < SW && pre[q][j].y != 0.0f);
+        if (lane == 0) {
+          const int sq = slot_rb + q;
+          vbits[(sq >= NR ? sq - NR : sq) * 8 + (c >> 5)] = bits;
+        }
       }
     __syncthreads();
     if (rb + kSBR < last) load_step(rb + kSBR);
@@ -542,29 +608,14 @@ __global__ void __launch_bounds__(256, 2) sep_strip(const SepArgs a) {
       const int q = 2 * warp + (lane >> 4);
       const int64_t gy = rb + q;
       if (gy < last) {
-        const int slot = static_cast<int>((gy - first) % NR);
+        const int slot = slot_rb + q >= NR ? slot_rb + q - NR : slot_rb + q;
         const int c0 = 8 * (lane & 15);
-        const float2* row = stg + q * PW;
+        // staged column c0 + i sits at strip_pos(c0 + i) = 9 (c0 / 8) + i + i / 8
+        const float2* row = stg + q * PW + 9 * (lane & 15);
         float2 acc[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) acc[u] = make_float2(0.0f, 0.0f);
-        float2 win[15];
-#pragma unroll
-        for (int j = 0; j < 7; ++j) win[j] = row[strip_pos(c0 + j)];
-        for (int t = 0; t < k; t += 8) {
-#pragma unroll
-          for (int j = 0; j < 8; ++j) win[7 + j] = row[strip_pos(c0 + t + 7 + j)];  // inside the padded row
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            if (t + j < k) {  // taps past k are never multiplied (their values may be NaN)
-              const float2 w = g2[t + j];
-#pragma unroll
-              for (int u = 0; u < 8; ++u) acc[u] = ffma2(w, win[u + j], acc[u]);
-            }
-          }
-#pragma unroll
-          for (int j = 0; j < 7; ++j) win[j] = win[8 + j];
-        }
+        taps8<KB>(g2, k, [&](int i) { return row[i + (i >> 3)]; }, acc);  // reads stay inside the padded row
         float2* dst_ring = ring + slot * kSTW2 + c0;
 #pragma unroll
         for (int u = 0; u < 8; u += 2)
@@ -584,38 +635,24 @@ __global__ void __launch_bounds__(256, 2) sep_strip(const SepArgs a) {
         float2 acc[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) acc[u] = make_float2(0.0f, 0.0f);
-        int sl = static_cast<int>((yb - r - first) % NR);
-        auto nxt = [&](int v) { return v + 1 == NR ? 0 : v + 1; };
-        float2 win[15];
-#pragma unroll
-        for (int j = 0; j < 7; ++j) {
-          win[j] = ring[sl * kSTW2 + c];
-          sl = nxt(sl);
-        }
-        for (int t = 0; t < k; t += 8) {
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            win[7 + j] = ring[sl * kSTW2 + c];  // slots past the window hold other rows: read, never used
-            sl = nxt(sl);
-          }
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            if (t + j < k) {
-              const float2 w = g2[t + j];
-#pragma unroll
-              for (int u = 0; u < 8; ++u) acc[u] = ffma2(w, win[u + j], acc[u]);
-            }
-          }
-#pragma unroll
-          for (int j = 0; j < 7; ++j) win[j] = win[8 + j];
-        }
+        const int sl0 = static_cast<int>(yb - r - first) % NR;  // < 512 + 2r rows into the segment
+        const float2* col = ring + c;
+        // ring row sl0 + i (wrapping once at most); slots past the window
+        // hold other rows: read, never multiplied
+        taps8<KB>(g2, k, [&](int i) {
+          const int sl = sl0 + i;
+          return col[(sl >= NR ? sl - NR : sl) * kSTW2];
+        }, acc);
         if (x < a.W) {
 #pragma unroll
           for (int u = 0; u < 8; ++u) {
             const int64_t y = yb + u;
             if (y >= ready_to) break;
-            // centre validity: its staged weight is 1 (in the raster and not nodata)
-            const bool centre_ok = strip_tap<DT>(src, a.dtype, y * a.pitch + x, a.nd).y != 0.0f;
+            // centre validity: its staged weight was 1 (in the raster and not nodata);
+            // row y = yb + u sits r + u slots after row yb - r
+            int sc = sl0 + r + u;
+            sc = sc >= NR ? sc - NR : sc;
+            const bool centre_ok = (vbits[sc * 8 + ((c + r) >> 5)] >> ((c + r) & 31)) & 1u;
             const float num = acc[u].x, den = acc[u].y;
             const bool ok = centre_ok && den > 0.0f;
             if (a.out_dtype == VSR_F64) static_cast<double*>(dst)[y * a.out_pitch + x] = ok ? static_cast<double>(num / den) : a.nd_out;
@@ -631,7 +668,11 @@ __global__ void __launch_bounds__(256, 2) sep_strip(const SepArgs a) {
 int launch_strip(const SepArgs& a, cudaStream_t st, int bands) {
   const size_t smem = strip_smem_bytes(a.k);
   if (smem > 227 * 1024) return fail(VSR_ERR_UNSUPPORTED, "Gaussian kernel %d too large for the strip kernel", a.k);
-  auto kern = a.dtype == VSR_U16 ? sep_strip<VSR_U16> : (a.dtype == VSR_F32 ? sep_strip<VSR_F32> : sep_strip<0>);
+  // the taps of k in 65..72 (sigma 8 at 4 sigma) are unrolled; other k run-time
+  const bool k9 = a.k > 64 && a.k <= 72;
+  auto kern = a.dtype == VSR_U16 ? (k9 ? sep_strip<VSR_U16, 9> : sep_strip<VSR_U16, 0>)
+              : a.dtype == VSR_F32 ? (k9 ? sep_strip<VSR_F32, 9> : sep_strip<VSR_F32, 0>)
+                                   : (k9 ? sep_strip<0, 9> : sep_strip<0, 0>);
   VSR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   dim3 grid(static_cast<unsigned>((a.W + kSTW2 - 1) / kSTW2), static_cast<unsigned>((a.H + kSSEG - 1) / kSSEG), bands);
   if (grid.y > 65535u) return fail(VSR_ERR_UNSUPPORTED, "raster too tall for the Gaussian grid");
