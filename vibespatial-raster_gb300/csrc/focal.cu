@@ -562,23 +562,42 @@ __global__ void __launch_bounds__(256, 2) sep_strip(const SepArgs a) {
   const int64_t first = ys - r;
   const int64_t last = ye + r;  // exclusive
   int64_t next_out = ys;
-  // staging: thread tid takes columns tid, tid + 256 of each of the kSBR
-  // rows; the next step's taps are loaded into registers during this
-  // step's passes
-  constexpr int kCols = 1;  // SW <= 128 + 79 < 256 threads
-  float2 pre[kSBR][kCols];
+  // staging: thread tid takes column tid (SW <= 128 + 79 < 256 threads) of
+  // each of the kSBR rows.  The next step's taps are loaded into registers
+  // during this step's passes and kept raw (uint16 / float; other dtypes
+  // converted at load), so nothing waits on the loads until the values are
+  // stored to shared memory at the start of the next step.
+  using Raw = std::conditional_t<DT == VSR_U16, uint32_t, std::conditional_t<DT == VSR_F32, float, float2>>;
+  Raw pre[kSBR];
+  uint32_t pin = 0;  // bit q: tap q of the staged step lies in the raster
+  const int c_st = tid;
   auto load_step = [&](int64_t rb) {
+    pin = 0;
+    const int64_t gx = x0 + c_st - r;
+    const bool col_in = c_st < SW && gx >= 0 && gx < a.W;
 #pragma unroll
     for (int q = 0; q < kSBR; ++q) {
       const int64_t gy = rb + q;
-      const bool row_in = gy < last && gy >= 0 && gy < a.H;
-#pragma unroll
-      for (int j = 0; j < kCols; ++j) {
-        const int c = tid + 256 * j;
-        const int64_t gx = x0 + c - r;
-        pre[q][j] = (row_in && c < SW && gx >= 0 && gx < a.W) ? strip_tap<DT>(src, a.dtype, gy * a.pitch + gx, a.nd)
-                                                              : make_float2(0.0f, 0.0f);
-      }
+      const bool in = col_in && gy < last && gy >= 0 && gy < a.H;
+      const int64_t idx = gy * a.pitch + gx;
+      if constexpr (DT == VSR_U16) pre[q] = in ? static_cast<uint32_t>(__ldg(static_cast<const uint16_t*>(src) + idx)) : 0u;
+      else if constexpr (DT == VSR_F32) pre[q] = in ? __ldg(static_cast<const float*>(src) + idx) : 0.0f;
+      else pre[q] = in ? strip_tap<DT>(src, a.dtype, idx, a.nd) : make_float2(0.0f, 0.0f);
+      pin |= (in ? 1u : 0u) << q;
+    }
+  };
+  // staged tap q as (v * valid, valid); NaN * 0 stays NaN (reference poisoning)
+  auto tap_of = [&](int q) -> float2 {
+    const bool in = (pin >> q) & 1u;
+    if constexpr (DT == VSR_U16) {
+      const bool ok = in && !(a.nd.kind == VSR_NODATA_VALUE && static_cast<int>(pre[q]) == a.nd.iv);
+      return make_float2(ok ? static_cast<float>(pre[q]) : 0.0f, ok ? 1.0f : 0.0f);
+    } else if constexpr (DT == VSR_F32) {
+      const float x = pre[q];
+      const bool ok = in && !(a.nd.kind == VSR_NODATA_VALUE ? x == a.nd.fv : (a.nd.kind == VSR_NODATA_NAN ? x != x : false));
+      return make_float2(x * (ok ? 1.0f : 0.0f), ok ? 1.0f : 0.0f);
+    } else {
+      return pre[q];
     }
   };
   load_step(first);
@@ -589,18 +608,16 @@ __global__ void __launch_bounds__(256, 2) sep_strip(const SepArgs a) {
     // row pass (before its column pass); the barrier below keeps this step's
     // row pass from overwriting ring rows the previous column pass reads.
 #pragma unroll
-    for (int q = 0; q < kSBR; ++q)
-#pragma unroll
-      for (int j = 0; j < kCols; ++j) {
-        const int c = tid + 256 * j;
-        if (c < SW) stg[q * PW + strip_pos(c)] = pre[q][j];
-        // validity of staged column c (the column pass reads its centres' bits)
-        const uint32_t bits = __ballot_sync(0xffffffffu, c < SW && pre[q][j].y != 0.0f);
-        if (lane == 0) {
-          const int sq = slot_rb + q;
-          vbits[(sq >= NR ? sq - NR : sq) * 8 + (c >> 5)] = bits;
-        }
+    for (int q = 0; q < kSBR; ++q) {
+      const float2 t = tap_of(q);
+      if (c_st < SW) stg[q * PW + strip_pos(c_st)] = t;
+      // validity of staged column c_st (the column pass reads its centres' bits)
+      const uint32_t bits = __ballot_sync(0xffffffffu, c_st < SW && t.y != 0.0f);
+      if (lane == 0) {
+        const int sq = slot_rb + q;
+        vbits[(sq >= NR ? sq - NR : sq) * 8 + (c_st >> 5)] = bits;
       }
+    }
     __syncthreads();
     if (rb + kSBR < last) load_step(rb + kSBR);
     // row pass: half-warp h takes staged row 2 warp + h, 8 columns per lane

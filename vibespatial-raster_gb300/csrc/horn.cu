@@ -272,6 +272,20 @@ __device__ __forceinline__ float grad_exact(float x0, float x2, float y0, float 
   return fabsf(g) <= 3.402823466e38f ? g : fmaf(2.0f, y2 - y0, (x2 - x0) + (z2 - z0));
 }
 
+// Three-input FP32 min / max (sm_100 and later; NaN inputs are ignored as by
+// fminf / fmaxf).  The exactness test's range only picks the gradient form,
+// so a NaN range simply selects the exact form.
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
 // Every difference (and the sums) of a row window is exact when all its
 // values lie in [m, 2m] for some m > 0, or in [-2m, -m], or are all zero.
 __device__ __forceinline__ bool window_exact(float lo, float hi) {
@@ -341,11 +355,11 @@ __device__ __forceinline__ void stage_row(const float* row, int lane, const Horn
       l[k] = nd ? __int_as_float(0x7f800000) : v[k];
       h[k] = nd ? __int_as_float(0xff800000) : v[k];
     }
-    lo = fminf(fminf(fminf(l[0], l[1]), fminf(l[2], l[3])), fminf(l[4], l[5]));
-    hi = fmaxf(fmaxf(fmaxf(h[0], h[1]), fmaxf(h[2], h[3])), fmaxf(h[4], h[5]));
+    lo = fminf(min3f(l[0], l[1], l[2]), min3f(l[3], l[4], l[5]));
+    hi = fmaxf(max3f(h[0], h[1], h[2]), max3f(h[3], h[4], h[5]));
   } else {
-    lo = fminf(fminf(fminf(v[0], v[1]), fminf(v[2], v[3])), fminf(v[4], v[5]));
-    hi = fmaxf(fmaxf(fmaxf(v[0], v[1]), fmaxf(v[2], v[3])), fmaxf(v[4], v[5]));
+    lo = fminf(min3f(v[0], v[1], v[2]), min3f(v[3], v[4], v[5]));
+    hi = fmaxf(max3f(v[0], v[1], v[2]), max3f(v[3], v[4], v[5]));
   }
 }
 
@@ -455,7 +469,7 @@ __device__ __forceinline__ void horn_rows(const float* S, int lane, int r0, int6
     stage_row<MASKED>(S + (r0 + j + 2) * kSW, lane, P, nd_in, skip_nd, v2, hd2, m2, lo2, hi2);
     stage_row<MASKED>(S + (r0 + j + 3) * kSW, lane, P, nd_in, skip_nd, v3, hd3, m3, lo3, hi3);
     // both output rows of the pair take the exact form if any lane's window may round
-    const float lo = fminf(fminf(lo0, lo1), fminf(lo2, lo3)), hi = fmaxf(fmaxf(hi0, hi1), fmaxf(hi2, hi3));
+    const float lo = fminf(min3f(lo0, lo1, lo2), lo3), hi = fmaxf(max3f(hi0, hi1, hi2), hi3);
     float* srow1 = (WANT & kWantSlope) ? srow + sp : nullptr;
     float* arow1 = (WANT & kWantAspect) ? arow + sp : nullptr;
     uint8_t* hrow1 = (WANT & kWantHs) ? hrow + hp : nullptr;
