@@ -178,6 +178,24 @@ def test_focal_mean_multiband_uint16_equals_per_band(vsr):
         np.testing.assert_array_equal(allb[i], oracle.focal_mean(stack[i], 3, 3, 0).astype(np.float32))
 
 
+@pytest.mark.parametrize("k", [35, 49, 79])
+def test_strip_gaussian_kernel_sizes(vsr, k):
+    """The strip kernel's ring depth and output-row groups depend on k: the
+    smallest strip size, a mid size and the largest Gaussian (run-time tap
+    loops), on 1100 rows (two full 512-row segments and a 76-row one whose
+    last output group holds 12 rows) and two 128-column strips."""
+    rng = np.random.default_rng(k)
+    shape = (1100, 200)
+    d = rng.integers(1, 10000, shape).astype(np.uint16)
+    d[rng.random(shape) < 0.03] = 0
+    sigma = k / 8.0
+    w = oracle.gaussian_weights(sigma, k)
+    assert w.shape == (k, k)
+    ref = oracle.convolve_normalized(d, w, 0)
+    out = vsr.raster_gaussian_filter(vsr.from_numpy(d, nodata=0), sigma, kernel_size=k, precision="fp32").to_numpy()
+    _assert_close(out, ref, d, 0)
+
+
 @pytest.mark.parametrize("dtype,nodata", [(np.float32, -9999.0), (np.uint16, 0), (np.float32, float("nan"))])
 def test_large_gaussian_strip_segments(vsr, dtype, nodata):
     """sigma 8, 65 x 65 on a raster taller than one 512-row segment and wider

@@ -452,9 +452,19 @@ constexpr int kSSEG = 512;  // rows per CTA segment
 
 __host__ __device__ inline int strip_pos(int i) { return i + (i >> 3); }  // conflict-free 8-wide lane strides
 __host__ __device__ inline int strip_pw(int k) { return strip_pos(kSTW2 + k + 7) + 1; }
+// Ring rows: output rows are produced in groups of 16 aligned to the segment
+// start; a group's k window rows plus the 15 rows staged past them must fit,
+// and with a multiple of 16 every window starts on a multiple of 8 slots,
+// so the ring wraps only between 8-row blocks.
+__host__ __device__ inline int strip_nr(int k) { return ((k - 1 + 15) & ~15) + kSBR; }
+// Position of column c in a ring row: column pairs XOR-swizzled inside each
+// group of 8 pairs, so the row pass's 16-byte stores (lane l: pairs 4l .. 4l+3)
+// spread over all banks while a warp's 32 consecutive columns in the column
+// pass still cover one contiguous 256-byte span.
+__device__ __forceinline__ int ring_pos(int c) { return c ^ (((c >> 4) & 7) << 1); }
 
 inline size_t strip_smem_bytes(int k) {
-  const int NR = k + kSBR - 1;
+  const int NR = strip_nr(k);
   const int k8 = (k + 7) & ~7;
   return (static_cast<size_t>(NR) * kSTW2 + static_cast<size_t>(kSBR) * strip_pw(k) + k8) * sizeof(float2) +
          static_cast<size_t>(NR) * 8 * 4 + 16;  // + validity bits of 256 staged columns per ring row
@@ -539,7 +549,7 @@ template <int DT, int KB>
 __global__ void __launch_bounds__(256, 2) sep_strip(const SepArgs a) {
   extern __shared__ __align__(16) float2 ssm2[];
   const int k = a.k, r = k / 2;
-  const int NR = k + kSBR - 1;
+  const int NR = strip_nr(k);
   const int PW = strip_pw(k);
   const int k8 = (k + 7) & ~7;
   float2* ring = ssm2;                  // NR x 128 (num, den) row-pass results
@@ -633,17 +643,21 @@ __global__ void __launch_bounds__(256, 2) sep_strip(const SepArgs a) {
 #pragma unroll
         for (int u = 0; u < 8; ++u) acc[u] = make_float2(0.0f, 0.0f);
         taps8<KB>(g2, k, [&](int i) { return row[i + (i >> 3)]; }, acc);  // reads stay inside the padded row
-        float2* dst_ring = ring + slot * kSTW2 + c0;
+        float2* dst_ring = ring + slot * kSTW2;
 #pragma unroll
         for (int u = 0; u < 8; u += 2)
-          *reinterpret_cast<float4*>(dst_ring + u) = make_float4(acc[u].x, acc[u].y, acc[u + 1].x, acc[u + 1].y);
+          *reinterpret_cast<float4*>(dst_ring + ring_pos(c0 + u)) =
+              make_float4(acc[u].x, acc[u].y, acc[u + 1].x, acc[u + 1].y);
       }
     }
     __syncthreads();
-    // column pass for the output rows whose window [y - r, y + r] is now in
-    // the ring (at most kSBR per step): 2 groups of 128 threads, 8 rows each
-    const int64_t ready_to = min(rb + kSBR - r, ye);  // outputs y < ready_to are complete
-    if (ready_to > next_out) {
+    // column pass: output rows in groups of 16 aligned to the segment start;
+    // a group runs once the last row of its last window (y - r + k - 1) is
+    // in the ring (one group per step, two at most at the segment end):
+    // 2 sets of 128 threads, 8 rows each
+    while (next_out < ye) {
+      const int64_t ready_to = min(next_out + kSBR, ye);
+      if (ready_to - 1 - r + k - 1 >= rb + kSBR) break;
       const int c = tid & (kSTW2 - 1);
       const int grp = tid >> 7;
       const int64_t x = x0 + c;
@@ -652,13 +666,16 @@ __global__ void __launch_bounds__(256, 2) sep_strip(const SepArgs a) {
         float2 acc[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) acc[u] = make_float2(0.0f, 0.0f);
-        const int sl0 = static_cast<int>(yb - r - first) % NR;  // < 512 + 2r rows into the segment
-        const float2* col = ring + c;
-        // ring row sl0 + i (wrapping once at most); slots past the window
-        // hold other rows: read, never multiplied
+        // slot of row yb - r: yb - ys is a multiple of 8 and NR of 16, so
+        // sl0 is a multiple of 8 and the window wraps (once at most) only
+        // between 8-row blocks: one slot test per block, the block's rows at
+        // fixed offsets.  Slots past the window hold other rows: read,
+        // never multiplied
+        const int sl0 = static_cast<int>(yb - r - first) % NR;
+        const float2* col = ring + ring_pos(c);
         taps8<KB>(g2, k, [&](int i) {
-          const int sl = sl0 + i;
-          return col[(sl >= NR ? sl - NR : sl) * kSTW2];
+          const int sb = sl0 + (i & ~7);
+          return col[((sb >= NR ? sb - NR : sb) + (i & 7)) * kSTW2];
         }, acc);
         if (x < a.W) {
 #pragma unroll
