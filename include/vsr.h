@@ -173,8 +173,25 @@ VSR_API int vsr_convolve_noalloc(const void* src, int dtype, int64_t height, int
  * weights outer(g, g) / sum exactly in real arithmetic, nodata and borders
  * included.  kernel_size <= 0 selects the default 2*ceil(3 sigma)+1; even
  * sizes are bumped to odd.  Same output rule as vsr_convolve.
+ *
+ * precision: VSR_PREC_FP32 runs the separable FP32 CUDA-core kernels.
+ * VSR_PREC_SPLIT_BF16 runs the two line passes on the tcgen05 tensor cores
+ * (8/16-bit integer rasters, kernel_size <= 79): each a GEMM against the
+ * Toeplitz band of the split weights (hi*hi + hi*lo + lo*hi, FP32
+ * accumulation), the row pass's sums kept as two float32 planes in the
+ * workspace.  Its hi/lo pairs are F16 (22 significant bits; a BF16 pair's
+ * 16 bits cannot carry the row pass's float32 sums to 2e-6).  VSR_PREC_AUTO takes the tensor cores for such rasters from
+ * kernel_size 35 when ``workspace_bytes`` covers
+ * vsr_gaussian_workspace_bytes, else the FP32 kernels.
+ *
+ * vsr_gaussian_workspace_size: the FP32 kernels' workspace (a few KB).
+ * vsr_gaussian_workspace_bytes: the workspace for a height x width raster of
+ * ``dtype`` at ``precision`` (the tensor-core passes need about 8 bytes per
+ * pixel); bands of a stack reuse it one after another.
  */
 VSR_API size_t vsr_gaussian_workspace_size(int kernel_size, int precision);
+VSR_API size_t vsr_gaussian_workspace_bytes(int64_t height, int64_t width, int dtype, double sigma,
+                                            int kernel_size, int precision);
 VSR_API int vsr_gaussian(const void* src, int dtype, int64_t height, int64_t width, int64_t pitch,
                  double sigma, int kernel_size, double nodata, int nodata_kind, void* dst,
                  int out_dtype, int64_t out_pitch, int precision, void* workspace,

@@ -1261,6 +1261,11 @@ int conv_tc_supported(int kh, int kw);
 int run_conv_tc(const void* src, int dtype, int64_t H, int64_t W, int64_t pitch, const double* weights_host,
                 int kh, int kw, double nodata, int nodata_kind, void* dst, int out_dtype, int64_t out_pitch,
                 void* workspace, size_t ws_bytes, cudaStream_t st);
+int gauss_tc_supported(int dtype, int k);  // gauss_tc.cu
+size_t gauss_tc_workspace(int64_t H, int64_t W, int dtype, int k);
+int run_gauss_tc(const void* src, int dtype, int bands, int64_t band_stride, int64_t H, int64_t W, int64_t pitch,
+                 double sigma, int k, double nodata, int nodata_kind, void* dst, int out_dtype,
+                 int64_t out_band_stride, int64_t out_pitch, void* workspace, size_t ws_bytes, cudaStream_t st);
 }  // namespace vsr
 
 extern "C" size_t vsr_convolve_workspace_size(int kh, int kw, int precision) {
@@ -1338,6 +1343,23 @@ extern "C" size_t vsr_gaussian_workspace_size(int kernel_size, int precision) {
   return gauss_ws(k);
 }
 
+// VSR_PREC_AUTO takes the split-BF16 line passes where the separable FP32
+// kernels would use the strip kernel (k > 33) on an 8/16-bit integer raster
+// (exact BF16 hi/lo values) and the caller's workspace holds their planes.
+static bool gauss_tc_auto(int dtype, int64_t height, int64_t width, int k, const void* workspace, size_t bytes) {
+  return k > kMaxSepK && gauss_tc_supported(dtype, k) && workspace && aligned(workspace, 256) &&
+         bytes >= gauss_tc_workspace(height, width, dtype, k);
+}
+
+extern "C" size_t vsr_gaussian_workspace_bytes(int64_t height, int64_t width, int dtype, double sigma,
+                                               int kernel_size, int precision) {
+  if (!(sigma > 0.0) || height < 0 || width < 0) return 0;
+  const int k = gaussian_size(sigma, kernel_size);
+  const bool tc = gauss_tc_supported(dtype, k) &&
+                  (precision == VSR_PREC_SPLIT_BF16 || (precision == VSR_PREC_AUTO && k > kMaxSepK));
+  return tc ? std::max(gauss_ws(k), gauss_tc_workspace(height, width, dtype, k)) : gauss_ws(k);
+}
+
 static int gaussian_impl(const void* src, int dtype, int bands, int64_t band_stride, int64_t height, int64_t width,
                          int64_t pitch, double sigma, int kernel_size, double nodata, int nodata_kind, void* dst,
                          int out_dtype, int64_t out_band_stride, int64_t out_pitch, int precision, void* workspace,
@@ -1347,9 +1369,12 @@ static int gaussian_impl(const void* src, int dtype, int bands, int64_t band_str
   int rc = check_raster(src, dtype, height, width, pitch, dst, out_dtype, out_pitch);
   if (rc || height == 0 || width == 0) return rc;
   if (precision < VSR_PREC_AUTO || precision > VSR_PREC_SPLIT_BF16) return fail(VSR_ERR_INVALID_ARG, "bad precision %d", precision);
-  if (precision == VSR_PREC_SPLIT_BF16) return fail(VSR_ERR_UNSUPPORTED, "split-BF16 Gaussian not in this build");
   const int k = gaussian_size(sigma, kernel_size);
   if (k > kMaxDirectK) return fail(VSR_ERR_UNSUPPORTED, "Gaussian kernel %d larger than %d", k, kMaxDirectK);
+  if (precision == VSR_PREC_SPLIT_BF16 || gauss_tc_auto(dtype, height, width, k, workspace, workspace_bytes))
+    return run_gauss_tc(src, dtype, bands, band_stride, height, width, pitch, sigma, k, nodata, nodata_kind, dst,
+                        out_dtype, out_band_stride, out_pitch, workspace, workspace_bytes,
+                        static_cast<cudaStream_t>(stream));
   const size_t need = gauss_ws(k);
   if (!workspace || workspace_bytes < need || !aligned(workspace, 256))
     return fail(VSR_ERR_WORKSPACE, "workspace must be 256-byte aligned and >= %zu bytes", need);

@@ -941,15 +941,6 @@ struct BatchSmem {
   static constexpr int kFloats = 2 * SR * kSW + 2 * SR * kTW;  // two staging buffers, row-pass sums
 };
 
-// 4-byte asynchronous global -> shared copy (any alignment of the source row).
-__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
 
 constexpr int kBatchSmemTiles = 2048;  // tiles whose prefix sums are searched in shared memory
 

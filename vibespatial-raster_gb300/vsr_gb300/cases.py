@@ -11,6 +11,8 @@ It is the small, single-kernel command to run under a profiler:
     focal_mean  uint16 band stack, gamma-like values 0..9999, 3 % nodata 0
                 (the 12 x 10980^2 multiband workload, fewer bands)
     gaussian    the same uint16 stack, Gaussian sigma / kernel size
+                (--precision split_bf16: the tensor-core line passes;
+                fp32: the separable CUDA-core kernels)
 
 Run with ``PYTHONPATH=vibespatial-raster_gb300`` from the repository root.
 """
@@ -83,8 +85,8 @@ def main(argv=None) -> None:
         if args.op == "focal_mean":
             fn = lambda: algebra.focal_mean_bands(r, args.radius, args.radius, out_dtype=np.float32, out=out)  # noqa: E731
         else:
-            fn = lambda: algebra.gaussian_bands(r, args.sigma, args.k, precision="auto", out_dtype=np.float32,  # noqa: E731
-                                                out=out)
+            fn = lambda: algebra.gaussian_bands(r, args.sigma, args.k, precision=args.precision,  # noqa: E731
+                                                out_dtype=np.float32, out=out)
         ms = _timed(fn, args.reps)
         px = args.bands * n * n
     print(json.dumps({"op": args.op, "size": n, "bands": args.bands, "ms": ms, "gpix_s": px / ms / 1e6,
