@@ -80,6 +80,10 @@ constexpr float kGScaleV = 0.5f;       // pass-1 values
 constexpr double kGScaleW = 4096.0;    // weights
 constexpr float kGScaleD = 256.0f;     // the row pass's weight sums
 constexpr uint32_t kF16One = 0x3c00u;  // 1.0 in F16
+// Pass-2 centre buffers: tile t's are copied at the start of iteration t and
+// read in its epilogue (iteration t + 2) up to the barrier opening iteration
+// t + 3's epilogue, so a buffer is rewritten four tiles later at the earliest.
+constexpr int kGCenBufs = 4;
 
 struct GaussGeom {
   int k, r;
@@ -120,7 +124,7 @@ struct GaussPlan {  // shared-memory byte offsets from the 1024-aligned base
   uint32_t xch;      // pass 2: 128 x kGXPitch floats (numerator rows over weight-sum rows);
                      // pass 1: the output staging, hi then lo, 8 chunks of kGStgChunk bytes each
   uint32_t raw;      // pass 1: 2 buffers x 64 rows x ngrp groups x 8 B of raw raster values;
-                     // pass 2: 3 buffers x 64 rows x 128 B of centre pixels
+                     // pass 2: kGCenBufs buffers x 64 rows x 128 B of centre pixels
   uint32_t total;
 };
 
@@ -131,7 +135,7 @@ __host__ __device__ inline GaussPlan gauss_plan(const GaussGeom& g, int pass) {
   p.band = 4 * p.a_bytes;
   p.xch = p.band + 2 * static_cast<uint32_t>(g.NB) * 128;
   p.raw = p.xch + (pass == 2 ? static_cast<uint32_t>(kMmaM) * kGXPitch * 4 : 2 * (kGL / 8) * kGStgChunk);
-  p.total = p.raw + (pass == 1 ? 2u * kGL * g.ngrp * 8 : 3u * kGL * 128);
+  p.total = p.raw + (pass == 1 ? 2u * kGL * g.ngrp * 8 : static_cast<uint32_t>(kGCenBufs) * kGL * 128);
   return p;
 }
 
@@ -308,16 +312,17 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
       return sm + L.raw + ((static_cast<uint32_t>(rb) * kGL + cw + kGWarps * q) * g.ngrp + grp) * 8;
     };
     auto copy_rows = [&](int rb, int64_t l0, int64_t p0) {
+      const int rows = static_cast<int>(a.lines - l0 < kGL ? a.lines - l0 : kGL);  // tile rows inside the raster
+      const int64_t rstep = kGWarps * a.pitch * kEsz;
       for (int grp = lane; grp < g.ngrp; grp += 32) {
         const int64_t xb = p0 - g.ra + 4 * grp;
-        const int64_t nin = xb < 0 ? 0 : (a.len - xb > 4 ? 4 : (a.len - xb > 0 ? a.len - xb : 0));
+        const int nin = xb < 0 ? 0 : static_cast<int>(a.len - xb > 4 ? 4 : (a.len - xb > 0 ? a.len - xb : 0));
+        const char* gp = static_cast<const char*>(a.src) + ((l0 + cw) * a.pitch + xb) * kEsz;
 #pragma unroll
-        for (int q = 0; q < kGLinesPerWarp; ++q) {
-          const int64_t y = l0 + cw + kGWarps * q;
-          const bool in = y < a.lines && nin > 0;
-          const void* gp = in ? static_cast<const void*>(static_cast<const char*>(a.src) + (y * a.pitch + xb) * kEsz)
-                              : a.src;
-          cp_async_zfill<4 * kEsz>(raw_slot(rb, q, grp), gp, in ? static_cast<uint32_t>(nin * kEsz) : 0u);
+        for (int q = 0; q < kGLinesPerWarp; ++q, gp += rstep) {
+          const bool in = cw + kGWarps * q < rows && nin > 0;
+          cp_async_zfill<4 * kEsz>(raw_slot(rb, q, grp), in ? static_cast<const void*>(gp) : a.src,
+                                   in ? static_cast<uint32_t>(nin * kEsz) : 0u);
         }
       }
     };
@@ -327,6 +332,7 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
     auto convert_rows = [&](int rb, int b, int64_t l0, int64_t p0) {
       unsigned char* ahi = sm + 2 * b * L.a_bytes;
       unsigned char* alo = ahi + L.a_bytes;
+      const int rows = static_cast<int>(a.lines - l0 < kGL ? a.lines - l0 : kGL);
       for (int grp = lane; grp < g.ngrp; grp += 32) {
         const int klo = g.Kp - 4 - 4 * grp;
         const uint32_t go = static_cast<uint32_t>(klo >> 3) * L.lbo + (klo & 7) * 2;
@@ -337,7 +343,7 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
 #pragma unroll
         for (int q = 0; q < kGLinesPerWarp; ++q) {
           const int i = cw + kGWarps * q;
-          if (l0 + i >= a.lines) continue;  // rows of lines past the raster are never stored
+          if (i >= rows) continue;  // rows of lines past the raster are never stored
           int v[4];
           if (DT == VSR_U8) {
             const uint32_t w = *reinterpret_cast<const uint32_t*>(raw_slot(rb, q, grp));
@@ -405,7 +411,15 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
     auto epilogue = [&](int jj, int64_t l0, int64_t p0, int cb) -> bool {
       const int b = jj & 1;
       const int64_t x2 = l0 + i2;
-      const bool got = wait_or_abort(&acc_full[b], (jj >> 1) & 1, &abort_flag, err_word, kDevErrMmaTimeout);
+      // one thread waits for the accumulators (and, pass 1, for the previous
+      // tile's output copies to have read the staging); the barrier-reduction
+      // orders the others after it -- and after their reads of the previous
+      // tile's exchange / staging -- and shares a failed wait
+      bool got = true;
+      if (ct == 0) {
+        got = wait_or_abort(&acc_full[b], (jj >> 1) & 1, &abort_flag, err_word, kDevErrMmaTimeout);
+        if (PASS == 1) bulk_wait_read<0>();
+      }
       if (g_any(!got)) return false;
       tc_fence_after();
       const int m = quarter * 32 + lane;
@@ -432,14 +446,13 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
         const int iy = m & (kGL - 1);
         const int64_t y = l0 + iy;
         unsigned char* stg = sm + L.xch;
-        if (ct == 0) bulk_wait_read<0>();  // the previous tile's copies have read the staging
-        g_sync();
         // chunk cl = 7 - iy / 8 of the tile (descending), element 7 - iy % 8
         const uint32_t o = (7 - iy / 8) * kGStgChunk + (m < kGL ? 0u : kGChunk / 2) + (7 - (iy & 7)) * 2;
         unsigned short* hrow = reinterpret_cast<unsigned short*>(stg + o);
         unsigned short* lrow = reinterpret_cast<unsigned short*>(stg + 8 * kGStgChunk + o);
         const float sc = m < kGL ? static_cast<float>(1.0 / kGScaleW) : static_cast<float>(kGScaleD / kGScaleW);
         const bool keep = y < a.lines;
+        const int cols = static_cast<int>(a.len - p0 < kGN ? a.len - p0 : kGN);  // lines x inside the raster
 #pragma unroll
         for (int h16 = 0; h16 < 2; ++h16) {
           float v[16];
@@ -447,7 +460,7 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
 #pragma unroll
           for (int n = 0; n < 16; ++n) {
             const int mx = half * 32 + 16 * h16 + n;
-            const float z = (keep && p0 + mx < a.len) ? v[n] * sc : 0.0f;
+            const float z = (keep && mx < cols) ? v[n] * sc : 0.0f;
             const __half hv = __float2half_rn(z);
             hrow[mx * 8] = __half_as_ushort(hv);
             lrow[mx * 8] = __half_as_ushort(__float2half_rn(z - __half2float(hv)));
@@ -474,7 +487,6 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
         }
       } else {
         float* xs = reinterpret_cast<float*>(sm + L.xch);
-        g_sync();  // the previous tile's exchange reads are done
 #pragma unroll
         for (int h16 = 0; h16 < 2; ++h16) {
           float v[16];
@@ -546,22 +558,17 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
           copy_rows((j + 1) & 1, lbn * kGL, (tn - lbn * npb) * kGN);
         }
       } else {
-        copy_centres(j % 3, l0, p0);
+        copy_centres(j % kGCenBufs, l0, p0);
       }
       cp_async_commit();
-      if (j >= 2 && !epilogue(j - 2, l2, p2, (j - 2) % 3)) {
+      if (j >= 2 && !epilogue(j - 2, l2, p2, (j - 2) % kGCenBufs)) {
         ok = false;
         break;
       }
       if (PASS == 1) {
+        // A buffer j&1 was last read by tile j-2's MMAs, complete once its
+        // accumulators were (the epilogue above waited for them)
         const int b = j & 1;
-        if (j >= 2) {
-          const bool got = wait_or_abort(&a_empty[b], ((j >> 1) - 1) & 1, &abort_flag, err_word, kDevErrMmaTimeout);
-          if (g_any(!got)) {
-            ok = false;
-            break;
-          }
-        }
         cp_async_wait<1>();  // tile j's raw copies have landed (tile j+1's may be in flight)
         convert_rows(j & 1, b, l0, p0);
         fence_proxy_async_smem();  // generic-proxy operand writes -> visible to the tensor core
@@ -576,11 +583,11 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
     // pass-2 wait count (at most 2 newer groups) right
     if (ok && j >= 2) {
       cp_async_commit();
-      ok = epilogue(j - 2, l2, p2, (j - 2) % 3);
+      ok = epilogue(j - 2, l2, p2, (j - 2) % kGCenBufs);
     }
     if (ok && j >= 1) {
       cp_async_commit();
-      epilogue(j - 1, l1, p1, (j - 1) % 3);
+      epilogue(j - 1, l1, p1, (j - 1) % kGCenBufs);
     }
     cp_async_wait<0>();
     if (PASS == 1 && ct == 0) bulk_wait_all();  // the output copies are done before the CTA ends
