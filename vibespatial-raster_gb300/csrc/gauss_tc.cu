@@ -416,10 +416,8 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
       // orders the others after it -- and after their reads of the previous
       // tile's exchange / staging -- and shares a failed wait
       bool got = true;
-      if (ct == 0) {
-        got = wait_or_abort(&acc_full[b], (jj >> 1) & 1, &abort_flag, err_word, kDevErrMmaTimeout);
-        if (PASS == 1) bulk_wait_read<0>();
-      }
+      if (PASS == 1 && ct < 16) bulk_wait_read<0>();  // this thread's chunk copy has read the staging
+      if (ct == 0) got = wait_or_abort(&acc_full[b], (jj >> 1) & 1, &abort_flag, err_word, kDevErrMmaTimeout);
       if (g_any(!got)) return false;
       tc_fence_after();
       const int m = quarter * 32 + lane;
@@ -432,7 +430,12 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
         tmem_wait_ld16(ra_);
         tmem_wait_ld16(rb_);
 #pragma unroll
-        for (int n = 0; n < 16; ++n) v[n] = __uint_as_float(ra_[n]) + __uint_as_float(rb_[n]);
+        for (int n = 0; n < 16; n += 2) {
+          const float2 sum = __fadd2_rn(make_float2(__uint_as_float(ra_[n]), __uint_as_float(ra_[n + 1])),
+                                        make_float2(__uint_as_float(rb_[n]), __uint_as_float(rb_[n + 1])));
+          v[n] = sum.x;
+          v[n + 1] = sum.y;
+        }
       };
       if (PASS == 1) {
         // P_num = sum g v/2, P_den = 2^8 sum g valid (the weight scale
@@ -458,30 +461,34 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
           float v[16];
           sums16(h16, v);
 #pragma unroll
-          for (int n = 0; n < 16; ++n) {
+          for (int n = 0; n < 16; n += 2) {  // two lines (rows mx, mx + 1 of the chunk) at a time
             const int mx = half * 32 + 16 * h16 + n;
-            const float z = (keep && mx < cols) ? v[n] * sc : 0.0f;
-            const __half hv = __float2half_rn(z);
-            hrow[mx * 8] = __half_as_ushort(hv);
-            lrow[mx * 8] = __half_as_ushort(__float2half_rn(z - __half2float(hv)));
+            const float2 z = __fmul2_rn(make_float2((keep && mx < cols) ? v[n] : 0.0f,
+                                                    (keep && mx + 1 < cols) ? v[n + 1] : 0.0f),
+                                        make_float2(sc, sc));
+            const __half2 hv = __floats2half2_rn(z.x, z.y);
+            const float2 rest = __fadd2_rn(z, make_float2(-__low2float(hv), -__high2float(hv)));
+            const __half2 lv = __floats2half2_rn(rest.x, rest.y);
+            hrow[mx * 8] = __half_as_ushort(__low2half(hv));
+            hrow[mx * 8 + 8] = __half_as_ushort(__high2half(hv));
+            lrow[mx * 8] = __half_as_ushort(__low2half(lv));
+            lrow[mx * 8 + 8] = __half_as_ushort(__high2half(lv));
           }
         }
         tc_fence_before();
         mbar_arrive(&acc_empty[b]);  // the accumulators may be reused
         fence_proxy_async_smem();    // generic-proxy staging writes -> visible to the bulk copies
         g_sync();
-        if (ct == 0) {
-          // chunk cl holds padded positions of chunk P = (l0 + ra)/8 + 7 - cl,
-          // stored at np - 1 - P of line block p0/64; chunks past round8(H) are skipped
+        if (ct < 16) {
+          // thread ct copies chunk cl = ct % 8 of plane ct / 8 (hi, lo): it holds
+          // padded positions of chunk P = (l0 + ra)/8 + 7 - cl, stored at
+          // np - 1 - P of line block p0/64; chunks past round8(H) are skipped
+          const int cl = ct & 7;
           const int64_t P0 = (l0 + g.ra) / 8;
-          unsigned char* gb = a.chi + (static_cast<size_t>(p0 / kGN) * a.np + (a.np - 1 - P0 - 7)) * kGChunk;
-          const size_t lo_off = static_cast<size_t>(a.clo - a.chi);
-          const int64_t h8 = (a.lines + 7) & ~int64_t(7);
-#pragma unroll 1
-          for (int cl = 0; cl < kGL / 8; ++cl) {
-            if (l0 + 8 * (7 - cl) >= h8) continue;
-            bulk_s2g(gb + cl * kGChunk, stg + cl * kGStgChunk, kGChunk);
-            bulk_s2g(gb + lo_off + cl * kGChunk, stg + (8 + cl) * kGStgChunk, kGChunk);
+          if (l0 + 8 * (7 - cl) < ((a.lines + 7) & ~int64_t(7))) {
+            unsigned char* gb = (ct < 8 ? a.chi : a.clo) +
+                                (static_cast<size_t>(p0 / kGN) * a.np + (a.np - 1 - P0 - 7 + cl)) * kGChunk;
+            bulk_s2g(gb, stg + ((ct >> 3) * 8 + cl) * kGStgChunk, kGChunk);
           }
           bulk_commit();
         }
@@ -590,7 +597,7 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
       epilogue(j - 1, l1, p1, (j - 1) % kGCenBufs);
     }
     cp_async_wait<0>();
-    if (PASS == 1 && ct == 0) bulk_wait_all();  // the output copies are done before the CTA ends
+    if (PASS == 1 && ct < 16) bulk_wait_all();  // the output copies are done before the CTA ends
   }
   __syncwarp();
   tc_fence_before();
