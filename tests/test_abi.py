@@ -64,3 +64,28 @@ def test_invalid_arguments_are_rejected_without_a_gpu(lib):
     # empty rasters are a no-op
     assert lib.vsr_horn_fused(None, _lib.VSR_F32, 0, 7, 7, 1.0, 1.0, 0.0, 0, 0, None, None, _lib.VSR_F32, 7,
                               None, 7, 1.0, 0.5, 0.5, None) == _lib.VSR_OK
+
+
+def test_gaussian_workspace_sizes(lib):
+    """The Gaussian's workspace query (host-only): the FP32 kernels need a few KB;
+    the tensor-core line passes (8/16-bit rasters; AUTO from k = 35) need their
+    two chunk planes -- 2 x 2 KB per 8 padded rows of each 64-column block -- plus
+    an aligned copy of one band."""
+    from vsr_gb300 import _lib
+
+    plain = lib.vsr_gaussian_workspace_size(65, _lib.VSR_PREC_FP32)
+    assert 0 < plain < 64 * 1024
+    H = W = 10980
+    # k = 65: windows of 64 + 64 positions (Kp = 128), 8-position chunks of 2 KB
+    np_chunks = ((H + 63) // 64 * 64 - 64 + 128) // 8
+    planes = 2 * ((W + 63) // 64) * np_chunks * 2048
+    tc = lib.vsr_gaussian_workspace_bytes(H, W, _lib.VSR_U16, 8.0, 65, _lib.VSR_PREC_AUTO)
+    assert planes < tc < planes + H * W * 2 + 64 * 1024
+    assert lib.vsr_gaussian_workspace_bytes(H, W, _lib.VSR_U16, 8.0, 65, _lib.VSR_PREC_SPLIT_BF16) == tc
+    # FP32 kernels: float rasters, explicit FP32, and AUTO below k = 35
+    for dt, k, prec in [(_lib.VSR_F32, 65, _lib.VSR_PREC_AUTO), (_lib.VSR_U16, 65, _lib.VSR_PREC_FP32),
+                        (_lib.VSR_U16, 33, _lib.VSR_PREC_AUTO)]:
+        assert lib.vsr_gaussian_workspace_bytes(H, W, dt, 8.0, k, prec) < 64 * 1024
+    # the default size from sigma (2 ceil(3 sigma) + 1 = 49) and invalid sigma
+    assert lib.vsr_gaussian_workspace_bytes(100, 100, _lib.VSR_U16, 8.0, 0, _lib.VSR_PREC_AUTO) > 64 * 1024
+    assert lib.vsr_gaussian_workspace_bytes(100, 100, _lib.VSR_U16, 0.0, 0, _lib.VSR_PREC_AUTO) == 0
