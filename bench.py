@@ -574,18 +574,72 @@ def run_slope2048(args, ws, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def run_derivatives(args, ws, rank, local):
+    """TRI + TPI + profile curvature in one pass over the 16384^2 fBm DEM (float64 out, the reference dtype)."""
+    import torch
+
+    import vsr_gb300 as vsr
+    from vsr_gb300 import algebra, workloads
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    vsr.load_library()
+    dem = workloads.terrain_16k(device=dev, size=args.dem_size)
+    H, W = dem.data.shape
+    r = vsr.from_device(dem.data, nodata=dem.nodata, affine=dem.affine)
+    outs = tuple(torch.empty((1, H, W), dtype=torch.float64, device=dev) for _ in range(3))
+    outs32 = tuple(torch.empty((1, H, W), dtype=torch.float32, device=dev) for _ in range(3))
+    stream = torch.cuda.current_stream()
+    fn = lambda: algebra.terrain_derivatives(r, out=outs)  # noqa: E731
+    for _ in range(max(3, args.warmup)):
+        fn()
+    steps = max(5, args.steps // 5)
+    ms = _time_ms(fn, steps, stream)
+    fn32 = lambda: algebra.terrain_derivatives(r, out_dtype=np.float32, out=outs32)  # noqa: E731
+    fn32()
+    ms32 = _time_ms(fn32, steps, stream)
+    hbm, _, src = _peaks()
+    import oracle  # CPU baseline only: the reference CPU algorithm, three calls
+
+    strip = dem.data[:512].cpu().numpy()
+    t0 = time.perf_counter()
+    for k in (oracle.TRI, oracle.TPI, oracle.CURVATURE):
+        oracle.terrain_derivative(strip, dem.affine, dem.nodata, k)
+    cpu_s = (time.perf_counter() - t0) / strip.size
+    px = H * W
+    line = {
+        "metric": METRIC, "value": px / (ms * 1e-3) / 1e9, "unit": UNIT, "n_gpus": ws, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 double-float (f64 out)", "data": "synthetic",
+        "config": {"workload": f"TRI + TPI + profile curvature, {H}x{W} f32 fBm DEM 0-4500 m, 10 m cells, "
+                               "200 -9999 disc holes; one pass, float64 outputs",
+                   "bytes_per_pixel": 28, "f32_outputs_ms": ms32,
+                   "l2": "1 GiB in + 6 GiB out per step exceed L2; no flush"},
+        "gpu_launches": steps,
+        "roofline": {"bound": "hbm", "achieved": 28 * px / (ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+                     "frac": 28 * px / (ms * 1e-3) / 1e9 / hbm, "traffic": None, "peak_source": src,
+                     "kernel": "terrain_deriv_kernel<float>"},
+        "cpu_baseline": {"value": 1.0 / cpu_s / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": "512 x 16384 rows of the same DEM, reference float64 TRI, TPI, curvature "
+                                   "(3 calls), 1 thread"},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["vsr", "reference"], default="vsr")
-    ap.add_argument("--workload", choices=["terrain", "slope2048", "conv", "batch", "multiband"], default="terrain",
+    ap.add_argument("--workload", choices=["terrain", "slope2048", "conv", "batch", "multiband", "derivatives"],
+                    default="terrain",
                     help="terrain (default, the headline): fused slope+aspect+hillshade on 16384^2; "
                          "conv: 8192^2 focal convolution, plain FP32 vs split-BF16; batch: 512 uneven tiles, "
                          "one graph-captured persistent launch vs per-tile launches; multiband: 12 x 10980^2 "
                          "uint16 focal mean 7x7 + Gaussian 65x65; slope2048: slope on a 2048^2 DEM vs the "
-                         "reference CPU fallback")
+                         "reference CPU fallback; derivatives: TRI + TPI + curvature on the 16384^2 DEM")
     ap.add_argument("--dem-size", type=int, default=16384,
                     help="DEM side (the benchmark workload is 16384; smaller sizes are for profiling)")
     args = ap.parse_args()
@@ -602,6 +656,8 @@ def main():
         run_multiband(args, ws, rank, local)
     elif args.workload == "slope2048":
         run_slope2048(args, ws, rank, local)
+    elif args.workload == "derivatives":
+        run_derivatives(args, ws, rank, local)
     else:
         run_vsr(args, ws, rank, local)
 

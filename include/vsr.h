@@ -123,6 +123,25 @@ VSR_API int vsr_horn_fused(const void* dem, int dtype, int64_t height, int64_t w
                    uint8_t* hillshade, int64_t hs_pitch, double z_factor, double zenith_rad,
                    double azimuth_rad, void* stream);
 
+/* ---- terrain derivatives: TRI, TPI, profile curvature -------------------
+ * Replaces the ``terrain_derivatives`` launches (algebra.py:2854-2991, kernel
+ * kernels/focal.py:487-647), one per derivative, with one pass for any subset,
+ * and their float64 up-cast and uint8 mask passes.  Semantics of
+ * algebra.py:3352-3445: edge-replicated 3x3 window z0..z8;
+ *   TRI = mean |z_i - z4|, TPI = z4 - mean z_i (the 8 neighbours),
+ *   curvature = -2 ((z3+z5)/2 - z4)/cx^2 + ((z1+z7)/2 - z4)/cy^2) * 100;
+ * border pixels and pixels whose window touches nodata get ``nodata_out``
+ * (the reference writes the raster's nodata, else -9999).  Outputs of
+ * ``out_dtype`` (the reference returns float64), row pitch ``out_pitch``; any
+ * of tri / tpi / curvature may be NULL.  8/16-bit and float32 DEMs are
+ * evaluated in double-float FP32 (error-free differences, compensated sums:
+ * ~44 significant bits), int32 and float64 DEMs in FP64.
+ */
+VSR_API int vsr_terrain_derivatives(const void* dem, int dtype, int64_t height, int64_t width, int64_t pitch,
+                                    double cell_x, double cell_y, double nodata, int nodata_kind,
+                                    double nodata_out, void* tri, void* tpi, void* curvature, int out_dtype,
+                                    int64_t out_pitch, void* stream);
+
 /* ---- nodata-aware normalised focal convolution --------------------------
  * Replaces the ``convolve_normalized`` launch (algebra.py:2077-2083, kernel
  * kernels/focal.py:36-146) with its up-cast, mask and weight-copy passes

@@ -14,6 +14,9 @@ the reference kernel plus the reference's known-answer tests.
 """
 
 from oracle.focal_oracle import (  # noqa: F401
+    CURVATURE,
+    TPI,
+    TRI,
     cellsize_from_affine,
     convolve_normalized,
     convolve_normalized_loop,
@@ -24,5 +27,6 @@ from oracle.focal_oracle import (  # noqa: F401
     nodata_ring,
     slope_aspect,
     slope_aspect_center_only,
+    terrain_derivative,
     terrain_out_dtype,
 )

@@ -208,6 +208,50 @@ def hillshade(data: np.ndarray, affine, nodata, *, azimuth=315.0, altitude=45.0,
 # ---------------------------------------------------------------------------
 
 
+TRI, TPI, CURVATURE = "tri", "tpi", "curvature"
+
+
+def terrain_derivative(data: np.ndarray, affine, nodata, kind: str) -> tuple[np.ndarray, float]:
+    """Reference CPU terrain derivative, algebra.py:3352-3445 (``_terrain_derivative_cpu``).
+
+    Returns (float64 output, output nodata value).  On the edge-padded float64
+    window z0..z8 (row-major, z4 the centre): TRI = mean |z_i - z4| over the 8
+    neighbours (Riley 1999), TPI = z4 - mean of the neighbours, profile
+    curvature (Zevenbergen & Thorne 1987) = -2 (D + E) 100 with
+    D = ((z3 + z5)/2 - z4) / cx^2, E = ((z1 + z7)/2 - z4) / cy^2.  Border pixels
+    and every pixel whose 3x3 window (constant-padded mask) touches nodata are
+    set to the output nodata: the raster's nodata, else -9999.0.
+    """
+    z = np.asarray(data).astype(np.float64)
+    if z.ndim == 3:
+        z = z[0]
+    h, w = z.shape
+    nd_out = float(nodata) if nodata is not None else -9999.0
+    p = np.pad(z, 1, mode="edge")
+    z0, z1, z2, z3, z4, z5, z6, z7, z8 = _shifted3x3(p)
+    if kind == TRI:
+        res = (np.abs(z0 - z4) + np.abs(z1 - z4) + np.abs(z2 - z4) + np.abs(z3 - z4) + np.abs(z5 - z4)
+               + np.abs(z6 - z4) + np.abs(z7 - z4) + np.abs(z8 - z4)) / 8.0
+    elif kind == TPI:
+        res = z4 - (z0 + z1 + z2 + z3 + z5 + z6 + z7 + z8) / 8.0
+    elif kind == CURVATURE:
+        cx, cy = cellsize_from_affine(affine)
+        d = ((z3 + z5) / 2.0 - z4) / (cx * cx)
+        e = ((z1 + z7) / 2.0 - z4) / (cy * cy)
+        res = -2.0 * (d + e) * 100.0
+    else:
+        raise ValueError(f"unknown terrain derivative {kind!r}")
+    out = np.full((h, w), nd_out, np.float64)
+    out[1:-1, 1:-1] = res[1:-1, 1:-1]
+    if nodata is not None:
+        m = np.pad(nodata_mask(z, nodata), 1, mode="constant", constant_values=False)
+        ring = np.zeros((h, w), bool)
+        for v in _shifted3x3(m):
+            ring |= v
+        out[ring] = nd_out
+    return out, nd_out
+
+
 def gaussian_weights(sigma: float, kernel_size: int | None = None) -> np.ndarray:
     """Reference Gaussian weights, algebra.py:2120-2152 (``raster_gaussian_filter``).
 

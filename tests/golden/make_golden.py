@@ -16,6 +16,8 @@ functions then run unmodified:
   -> ``_hillshade_cpu``           (algebra.py:2543-2629)
 * ``raster_focal_mean`` with ``use_gpu=False``
   -> ``_focal_mean_cpu``          (algebra.py:3083-3101)
+* ``raster_tri`` / ``raster_tpi`` / ``raster_curvature`` with ``use_gpu=False``
+  -> ``_terrain_derivative_cpu``  (algebra.py:3352-3445)
 * ``raster_gaussian_filter`` / ``raster_convolve`` weight handling
   (algebra.py:2101-2154): the reference has no CPU convolution, so the
   weights it hands to ``_gpu_convolve`` are captured by replacing that one
@@ -236,6 +238,13 @@ def main() -> None:
             arrays[f"terrain/{name}/hillshade{k}"] = hs.to_numpy()
             if k == 0:
                 hs_nodata = hs.nodata
+        deriv_nodata = None
+        for key, fn in (("tri", ref_alg.raster_tri), ("tpi", ref_alg.raster_tpi),
+                        ("curvature", ref_alg.raster_curvature)):
+            with np.errstate(invalid="ignore"):
+                dv = fn(dem, use_gpu=False)
+            arrays[f"terrain/{name}/{key}"] = dv.to_numpy()
+            deriv_nodata = dv.nodata
         manifest["terrain"].append(
             {
                 "name": name,
@@ -244,6 +253,7 @@ def main() -> None:
                 "in_dtype": str(c["data"].dtype),
                 "slope_dtype": str(s.dtype),
                 "hillshade_nodata": hs_nodata,
+                "deriv_nodata": deriv_nodata,
             }
         )
 

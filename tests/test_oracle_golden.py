@@ -2,7 +2,8 @@
 
 The fixtures come from tests/golden/make_golden.py, which runs
 vibespatial-raster 0.1.7's ``_cpu_slope_aspect`` / ``_hillshade_cpu`` /
-``_focal_mean_cpu`` and captures the Gaussian weights it builds.  CPU only.
+``_focal_mean_cpu`` / ``_terrain_derivative_cpu`` and captures the Gaussian
+weights it builds.  CPU only.
 """
 
 from __future__ import annotations
@@ -33,6 +34,22 @@ def test_oracle_slope_aspect_matches_reference(golden):
         # identical float64 arithmetic -> bit-identical after the same cast
         np.testing.assert_array_equal(s.astype(dt), ref_s, err_msg=name)
         np.testing.assert_array_equal(a.astype(dt), ref_a, err_msg=name)
+
+
+def test_oracle_terrain_derivatives_match_reference(golden):
+    """TRI, TPI and profile curvature bit for bit against the reference's
+    ``_terrain_derivative_cpu`` (borders and dilated nodata set to the raster's
+    nodata, else -9999)."""
+    arrays, manifest = golden
+    for case in manifest["terrain"]:
+        name = case["name"]
+        data = arrays[f"terrain/{name}/input"]
+        for kind in (oracle.TRI, oracle.TPI, oracle.CURVATURE):
+            with np.errstate(invalid="ignore"):
+                out, nd = oracle.terrain_derivative(data, case["affine"], case["nodata"], kind)
+            np.testing.assert_array_equal(out, arrays[f"terrain/{name}/{kind}"], err_msg=f"{name} {kind}")
+            ref_nd = case["deriv_nodata"]
+            assert (np.isnan(nd) and np.isnan(ref_nd)) or nd == ref_nd, name
 
 
 def test_oracle_hillshade_matches_reference(golden):

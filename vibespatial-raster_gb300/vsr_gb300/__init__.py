@@ -12,11 +12,15 @@ from vsr_gb300._lib import load as load_library  # noqa: F401
 from vsr_gb300.algebra import (  # noqa: F401
     raster_aspect,
     raster_convolve,
+    raster_curvature,
     raster_focal_mean,
     raster_gaussian_filter,
     raster_hillshade,
     raster_slope,
     raster_terrain,
+    raster_terrain_derivatives,
+    raster_tpi,
+    raster_tri,
 )
 from vsr_gb300.buffers import (  # noqa: F401
     OwnedRasterArray,
@@ -40,9 +44,13 @@ __all__ = [
     "load_library",
     "raster_aspect",
     "raster_convolve",
+    "raster_curvature",
     "raster_focal_mean",
     "raster_gaussian_filter",
     "raster_hillshade",
     "raster_slope",
     "raster_terrain",
+    "raster_terrain_derivatives",
+    "raster_tpi",
+    "raster_tri",
 ]

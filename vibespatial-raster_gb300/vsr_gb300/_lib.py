@@ -59,6 +59,10 @@ SIGNATURES: dict[str, tuple] = {
         [_vp, _int, _i64, _i64, _i64, _dbl, _dbl, _dbl, _int, _u32, _vp, _vp, _int, _i64, _vp, _i64,
          _dbl, _dbl, _dbl, _vp],
     ),
+    "vsr_terrain_derivatives": (
+        _int,
+        [_vp, _int, _i64, _i64, _i64, _dbl, _dbl, _dbl, _int, _dbl, _vp, _vp, _vp, _int, _i64, _vp],
+    ),
     "vsr_convolve_workspace_size": (_sz, [_int, _int, _int]),
     "vsr_convolve": (
         _int,

@@ -274,6 +274,87 @@ def raster_terrain(dem: OwnedRasterArray, *, slope: bool = True, aspect: bool = 
 _PRECISION = {"auto": _lib.VSR_PREC_AUTO, "fp32": _lib.VSR_PREC_FP32, "split_bf16": _lib.VSR_PREC_SPLIT_BF16}
 
 
+# ---------------------------------------------------------------------------
+# Terrain derivatives (TRI, TPI, profile curvature)
+# ---------------------------------------------------------------------------
+
+_DERIV_NAMES = {"tri": "TRI", "tpi": "TPI", "curvature": "curvature"}
+
+
+def derivative_nodata(dem: OwnedRasterArray) -> float:
+    """Output nodata of the terrain derivatives: the raster's, else -9999 (algebra.py:3376)."""
+    return float(dem.nodata) if dem.nodata is not None else -9999.0
+
+
+def terrain_derivatives(dem: OwnedRasterArray, *, tri: bool = True, tpi: bool = True, curvature: bool = True,
+                        out_dtype=np.float64, out=None):
+    """Launch vsr_terrain_derivatives over every band; returns (tri, tpi, curvature) (B, H, W) tensors.
+
+    ``out`` may supply preallocated device tensors (None entries are allocated).
+    """
+    torch = _torch()
+    src, dt = _device_bands(dem)
+    B, H, W = src.shape
+    kind, ndv = nodata_kind(dem)
+    ocode, odt = _out_code(out_dtype)
+    o_t, o_p, o_c = out if out is not None else (None, None, None)
+    dev = src.device
+    mk = lambda o, want: (o if o is not None else torch.empty((B, H, W), dtype=torch_dtype(odt), device=dev)) if want else None  # noqa: E731
+    t_t, p_t, c_t = mk(o_t, tri), mk(o_p, tpi), mk(o_c, curvature)
+    cx, cy = cellsize(dem.affine)
+    lib = _lib.load()
+    stream = _stream_handle()
+    esz = src.element_size()
+    for b in range(B):
+        st = lib.vsr_terrain_derivatives(
+            src.data_ptr() + b * H * W * esz, _lib.dtype_code(dt), H, W, W, cx, cy, ndv, kind,
+            derivative_nodata(dem),
+            t_t[b].data_ptr() if t_t is not None else None,
+            p_t[b].data_ptr() if p_t is not None else None,
+            c_t[b].data_ptr() if c_t is not None else None,
+            ocode, W, stream,
+        )
+        _lib.check(st, "vsr_terrain_derivatives")
+    return t_t, p_t, c_t
+
+
+def raster_terrain_derivatives(dem: OwnedRasterArray, *, tri: bool = True, tpi: bool = True,
+                               curvature: bool = True, use_gpu: bool | None = None) -> dict[str, OwnedRasterArray]:
+    """TRI, TPI and profile curvature from one pass over the DEM.
+
+    Each result equals what raster_tri / raster_tpi / raster_curvature return
+    for the same DEM (float64, nodata = the raster's, else -9999); returns a dict
+    with the requested keys.
+    """
+    _require_gpu(use_gpu)
+    t0 = time.perf_counter()
+    ts = terrain_derivatives(dem, tri=tri, tpi=tpi, curvature=curvature)
+    el = time.perf_counter() - t0
+    nd = derivative_nodata(dem)
+    res = {}
+    for key, t in zip(("tri", "tpi", "curvature"), ts):
+        if t is None:
+            continue
+        r = from_device(_shape_like(dem, t), nodata=nd, affine=dem.affine, crs=dem.crs)
+        res[key] = _record(r, f"gpu_terrain_{_DERIV_NAMES[key]} {dem.width}x{dem.height}", el)
+    return res
+
+
+def raster_tri(dem: OwnedRasterArray, *, use_gpu: bool | None = None) -> OwnedRasterArray:
+    """Terrain Ruggedness Index (mean |z_i - z4| over the 8 neighbours), reference algebra.py:3448-3471."""
+    return raster_terrain_derivatives(dem, tri=True, tpi=False, curvature=False, use_gpu=use_gpu)["tri"]
+
+
+def raster_tpi(dem: OwnedRasterArray, *, use_gpu: bool | None = None) -> OwnedRasterArray:
+    """Topographic Position Index (z4 - mean of the 8 neighbours), reference algebra.py:3474-3498."""
+    return raster_terrain_derivatives(dem, tri=False, tpi=True, curvature=False, use_gpu=use_gpu)["tpi"]
+
+
+def raster_curvature(dem: OwnedRasterArray, *, use_gpu: bool | None = None) -> OwnedRasterArray:
+    """Profile curvature (Zevenbergen & Thorne 1987), reference algebra.py:3501-3525."""
+    return raster_terrain_derivatives(dem, tri=False, tpi=False, curvature=True, use_gpu=use_gpu)["curvature"]
+
+
 def _precision_code(precision: str) -> int:
     try:
         return _PRECISION[precision]
