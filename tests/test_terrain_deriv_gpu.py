@@ -70,7 +70,8 @@ def test_matches_oracle(vsr, dtype, nodata):
 
 
 def test_non_finite_values_propagate(vsr):
-    """Without nodata, NaN and +-inf enter the arithmetic as in the reference."""
+    """Without nodata, NaN and +-inf enter the arithmetic as in the reference; a
+    non-finite corner leaves the curvature (which does not read corners) exact."""
     rng = np.random.default_rng(9)
     d = rng.uniform(100, 200, (40, 45)).astype(np.float32)
     d[10, 10] = np.nan
@@ -107,9 +108,9 @@ def test_api_contract(vsr):
     r = vsr.from_numpy(d)
     tri = vsr.raster_tri(r)
     assert tri.nodata == -9999.0 and tri.to_numpy().dtype == np.float64
-    assert tri.diagnostics[-1].detail.startswith("gpu_terrain_TRI 6x6")
-    assert vsr.raster_tpi(r).diagnostics[-1].detail.startswith("gpu_terrain_TPI")
-    assert vsr.raster_curvature(r).diagnostics[-1].detail.startswith("gpu_terrain_curvature")
+    assert any(e.detail.startswith("gpu_terrain_TRI 6x6") for e in tri.diagnostics)
+    assert any(e.detail.startswith("gpu_terrain_TPI") for e in vsr.raster_tpi(r).diagnostics)
+    assert any(e.detail.startswith("gpu_terrain_curvature") for e in vsr.raster_curvature(r).diagnostics)
     # a plane: TPI and curvature 0 inside, TRI = mean |neighbour step|
     np.testing.assert_array_equal(vsr.raster_tpi(r).to_numpy()[1:-1, 1:-1], 0.0)
     np.testing.assert_array_equal(vsr.raster_curvature(r).to_numpy()[1:-1, 1:-1], 0.0)

@@ -19,9 +19,9 @@
 // formed error-free (TwoDiff), sums are compensated (TwoSum) and products use
 // FMA, so results carry ~44 significant bits -- float64 quality for these
 // few-term formulas -- before the single conversion to the output type.
-// Windows with non-finite values take the plain float formulas (NaN and
-// +-inf propagate as in the reference).  int32 and float64 DEMs are computed
-// in FP64 with the reference's own operation order.
+// A formula whose inputs include NaN or +-inf takes the plain float form
+// (the special values propagate as in the reference).  int32 and float64
+// DEMs are computed in FP64 with the reference's own operation order.
 #include <cmath>
 #include <type_traits>
 
@@ -92,6 +92,26 @@ __device__ __forceinline__ void store_df(void* base, int out_dtype, int64_t i, D
   else static_cast<float*>(base)[i] = v.hi + v.lo;
 }
 
+// The reference's formulas in the operation order of algebra.py:3394-3412
+// (double for FP64 DEMs; float where a window holds NaN or +-inf, whose
+// special values propagate the same way in either precision).
+template <typename C>
+__device__ __forceinline__ C plain_tri(const C z[9]) {
+  return (fabs(z[0] - z[4]) + fabs(z[1] - z[4]) + fabs(z[2] - z[4]) + fabs(z[3] - z[4]) + fabs(z[5] - z[4]) +
+          fabs(z[6] - z[4]) + fabs(z[7] - z[4]) + fabs(z[8] - z[4])) /
+         C(8);
+}
+template <typename C>
+__device__ __forceinline__ C plain_tpi(const C z[9]) {
+  return z[4] - (z[0] + z[1] + z[2] + z[3] + z[5] + z[6] + z[7] + z[8]) / C(8);
+}
+template <typename C>
+__device__ __forceinline__ C plain_curv(const C z[9], const DerivParams& P) {
+  const C D = ((z[3] + z[5]) / C(2) - z[4]) / static_cast<C>(P.cx2);
+  const C E = ((z[1] + z[7]) / C(2) - z[4]) / static_cast<C>(P.cy2);
+  return C(-2) * (D + E) * C(100);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kDTW * kDTH) terrain_deriv_kernel(const T* __restrict__ src, const DerivParams P) {
   constexpr bool kDF = !std::is_same<T, double>::value && !std::is_same<T, int32_t>::value;
@@ -129,51 +149,56 @@ __global__ void __launch_bounds__(kDTW * kDTH) terrain_deriv_kernel(const T* __r
     if (P.curv) store_out(P.curv, P.out_dtype, o, P.nd_out);
     return;
   }
-  bool finite = true;
+  // finiteness of the values each formula reads: TRI and TPI all nine,
+  // curvature the centre and its four edge neighbours
+  bool f5 = true, f9;
 #pragma unroll
-  for (int k = 0; k < 9; ++k) finite &= fabs(z[k]) <= static_cast<C>(3.4e38);
-  if (kDF && finite) {
+  for (int k = 1; k < 9; k += 2) f5 &= fabs(z[k]) <= static_cast<C>(3.4e38);
+  f5 &= fabs(z[4]) <= static_cast<C>(3.4e38);
+  f9 = f5 && fabs(z[0]) <= static_cast<C>(3.4e38) && fabs(z[2]) <= static_cast<C>(3.4e38) &&
+       fabs(z[6]) <= static_cast<C>(3.4e38) && fabs(z[8]) <= static_cast<C>(3.4e38);
+  if (kDF) {
     // error-free neighbour differences d_i = z_i - z4 (i = 0..3, 5..8)
     DF d[8];
 #pragma unroll
     for (int k = 0, i = 0; k < 9; ++k)
       if (k != 4) d[i++] = two_diff_df(static_cast<float>(z[k]), static_cast<float>(z[4]));
     if (P.tri) {
-      DF s = df_abs(d[0]);
+      if (f9) {
+        DF s = df_abs(d[0]);
 #pragma unroll
-      for (int i = 1; i < 8; ++i) s = df_add(s, df_abs(d[i]));
-      store_df(P.tri, P.out_dtype, o, df_scale(s, 0.125f));
+        for (int i = 1; i < 8; ++i) s = df_add(s, df_abs(d[i]));
+        store_df(P.tri, P.out_dtype, o, df_scale(s, 0.125f));
+      } else {
+        store_out(P.tri, P.out_dtype, o, plain_tri(z));
+      }
     }
     if (P.tpi) {
-      DF s = d[0];
+      if (f9) {
+        DF s = d[0];
 #pragma unroll
-      for (int i = 1; i < 8; ++i) s = df_add(s, d[i]);
-      store_df(P.tpi, P.out_dtype, o, df_scale(df_neg(s), 0.125f));  // z4 - mean = -(sum d_i) / 8
+        for (int i = 1; i < 8; ++i) s = df_add(s, d[i]);
+        store_df(P.tpi, P.out_dtype, o, df_scale(df_neg(s), 0.125f));  // z4 - mean = -(sum d_i) / 8
+      } else {
+        store_out(P.tpi, P.out_dtype, o, plain_tpi(z));
+      }
     }
     if (P.curv) {
-      // (z3 + z5)/2 - z4 = (d_w + d_e) / 2, (z1 + z7)/2 - z4 = (d_n + d_s) / 2
-      const DF dx = df_scale(df_add(d[3], d[4]), 0.5f), dy = df_scale(df_add(d[1], d[6]), 0.5f);
-      const DF e = df_add(df_mul(dx, DF{P.icx2_hi, P.icx2_lo}), df_mul(dy, DF{P.icy2_hi, P.icy2_lo}));
-      store_df(P.curv, P.out_dtype, o, df_mul_f(e, -200.0f));
+      if (f5) {
+        // (z3 + z5)/2 - z4 = (d_w + d_e) / 2, (z1 + z7)/2 - z4 = (d_n + d_s) / 2
+        const DF dx = df_scale(df_add(d[3], d[4]), 0.5f), dy = df_scale(df_add(d[1], d[6]), 0.5f);
+        const DF e = df_add(df_mul(dx, DF{P.icx2_hi, P.icx2_lo}), df_mul(dy, DF{P.icy2_hi, P.icy2_lo}));
+        store_df(P.curv, P.out_dtype, o, df_mul_f(e, -200.0f));
+      } else {
+        store_out(P.curv, P.out_dtype, o, plain_curv(z, P));
+      }
     }
     return;
   }
-  // FP64 DEMs, int32 DEMs, and windows holding non-finite values: the
-  // reference's formulas in C (double, or float with propagating NaN / inf)
-  if (P.tri) {
-    const C t = (fabs(z[0] - z[4]) + fabs(z[1] - z[4]) + fabs(z[2] - z[4]) + fabs(z[3] - z[4]) +
-                 fabs(z[5] - z[4]) + fabs(z[6] - z[4]) + fabs(z[7] - z[4]) + fabs(z[8] - z[4])) / C(8);
-    store_out(P.tri, P.out_dtype, o, t);
-  }
-  if (P.tpi) {
-    const C m = (z[0] + z[1] + z[2] + z[3] + z[5] + z[6] + z[7] + z[8]) / C(8);
-    store_out(P.tpi, P.out_dtype, o, z[4] - m);
-  }
-  if (P.curv) {
-    const C D = ((z[3] + z[5]) / C(2) - z[4]) / static_cast<C>(P.cx2);
-    const C E = ((z[1] + z[7]) / C(2) - z[4]) / static_cast<C>(P.cy2);
-    store_out(P.curv, P.out_dtype, o, C(-2) * (D + E) * C(100));
-  }
+  // FP64 DEMs and int32 DEMs: the reference's formulas in double
+  if (P.tri) store_out(P.tri, P.out_dtype, o, plain_tri(z));
+  if (P.tpi) store_out(P.tpi, P.out_dtype, o, plain_tpi(z));
+  if (P.curv) store_out(P.curv, P.out_dtype, o, plain_curv(z, P));
 }
 
 template <typename T>
