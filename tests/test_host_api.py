@@ -33,6 +33,23 @@ def test_use_gpu_false_raises_no_cpu_path():
         vsr.raster_hillshade(r, use_gpu=False)
 
 
+def test_terrain_derivative_api_matches_reference():
+    """raster_tri / raster_tpi / raster_curvature(dem, *, use_gpu=None)
+    (algebra.py:3448-3525); output nodata = the raster's, else -9999
+    (algebra.py:3376); GPU only."""
+    for fn in (vsr.raster_tri, vsr.raster_tpi, vsr.raster_curvature):
+        p = inspect.signature(fn).parameters
+        assert list(p) == ["dem", "use_gpu"] and p["use_gpu"].default is None
+        assert p["use_gpu"].kind is inspect.Parameter.KEYWORD_ONLY
+    r = vsr.from_numpy(np.zeros((4, 4), np.float32))
+    for fn in (vsr.raster_tri, vsr.raster_tpi, vsr.raster_curvature, vsr.raster_terrain_derivatives):
+        with pytest.raises(NotImplementedError):
+            fn(r, use_gpu=False)
+    assert algebra.derivative_nodata(r) == -9999.0
+    assert algebra.derivative_nodata(vsr.from_numpy(np.zeros((4, 4), np.int16), nodata=-32768)) == -32768.0
+    assert np.isnan(algebra.derivative_nodata(vsr.from_numpy(np.zeros((4, 4), np.float32), nodata=float("nan"))))
+
+
 def test_cellsize_rule():
     # |a|, |e|, 1.0 for zero; rotation ignored (algebra.py:2307-2308)
     assert algebra.cellsize((-2.0, 0.5, 0.0, 0.3, 3.0, 0.0)) == (2.0, 3.0)
