@@ -716,15 +716,9 @@ int launch_strip(const SepArgs& a, cudaStream_t st, int bands) {
 }
 
 // ------------------------------------------------------------- box_mean --
-// Accumulators: exact int32 sums (<= 16-bit integer rasters), float TwoSum
-// pairs (float32), float64 (float64 / int32 rasters).
-struct AccI {
-  int32_t s;
-  __device__ void zero() { s = 0; }
-  __device__ void add(int32_t v) { s += v; }
-  __device__ void add(const AccI& o) { s += o.s; }
-  __device__ double value() const { return static_cast<double>(s); }
-};
+// Accumulators of the general kernel: float TwoSum pairs (float32 rasters),
+// float64 (everything else; 8/16-bit rasters reach it only for windows too
+// large for the exact integer kernels).
 struct AccF2 {
   float s, c;
   __device__ void zero() { s = 0.0f; c = 0.0f; }
