@@ -15,12 +15,14 @@ the reference kernel plus the reference's known-answer tests.
 
 from oracle.focal_oracle import (  # noqa: F401
     CURVATURE,
+    FOCAL_STATS,
     TPI,
     TRI,
     cellsize_from_affine,
     convolve_normalized,
     convolve_normalized_loop,
     focal_mean,
+    focal_stat,
     gaussian_weights,
     hillshade,
     nodata_mask,

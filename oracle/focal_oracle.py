@@ -346,6 +346,69 @@ def convolve_normalized_loop(data: np.ndarray, weights: np.ndarray, nodata) -> n
 # ---------------------------------------------------------------------------
 
 
+FOCAL_STATS = ("min", "max", "mean", "std", "range", "variety")
+
+
+def focal_stat(data: np.ndarray, radius_y: int, radius_x: int, nodata, stat: str) -> np.ndarray:
+    """Reference CPU focal statistics, algebra.py:3041-3164 (``_focal_{stat}_cpu``) via
+    ``_focal_stat_cpu`` (:3177-3213).  float64.
+
+    Over the in-bounds taps of the (2ry+1) x (2rx+1) window (out-of-bounds
+    taps are the placeholder):
+      min / max  nodata -> +inf / -inf placeholders, excluded with every tap
+                 equal to the placeholder (valid +-inf data too); NaN data
+                 propagates;
+      mean, std (population), range, variety (count of distinct values)
+                 nodata -> NaN placeholder, excluded with NaN data.
+    A window with no valid tap gives the nodata value (0.0 when the raster has
+    none, :3196) -- 0.0 for std and variety; a nodata centre gives the nodata
+    value.  Evaluated on sliding-window views (mean and std sum in another
+    order than the reference: agreement within ~1e-13 relative).
+    """
+    from numpy.lib.stride_tricks import sliding_window_view
+
+    if stat not in FOCAL_STATS:
+        raise ValueError(f"unknown focal statistic {stat!r}")
+    z = np.asarray(data).astype(np.float64)
+    if z.ndim == 3:
+        z = z[0]
+    nd = nodata_mask(np.asarray(data), nodata) if nodata is not None else np.zeros(z.shape, bool)
+    nd_val = float(nodata) if nodata is not None else 0.0
+    ph = {"min": np.inf, "max": -np.inf}.get(stat, np.nan)
+    work = np.where(nd, ph, z)
+    pad = np.pad(work, ((radius_y, radius_y), (radius_x, radius_x)), mode="constant", constant_values=ph)
+    win = sliding_window_view(pad, (2 * radius_y + 1, 2 * radius_x + 1)).reshape(z.shape + (-1,))
+    with np.errstate(invalid="ignore"):
+        if stat in ("min", "max"):
+            excl = win == ph
+            nvalid = (~excl).sum(axis=-1)
+            has_nan = np.isnan(win).any(axis=-1)
+            fill = np.where(excl | np.isnan(win), ph, win)
+            out = fill.min(axis=-1) if stat == "min" else fill.max(axis=-1)
+            out = np.where(has_nan, np.nan, out)
+            out = np.where(nvalid > 0, out, nd_val)
+        else:
+            ok = ~np.isnan(win)
+            nvalid = ok.sum(axis=-1)
+            if stat == "mean":
+                out = np.where(nvalid > 0, np.nanmean(np.where(nvalid[..., None] > 0, win, 0.0), axis=-1), nd_val)
+            elif stat == "std":
+                out = np.where(nvalid > 0, np.nanstd(np.where(nvalid[..., None] > 0, win, 0.0), axis=-1), 0.0)
+            elif stat == "range":
+                lo = np.where(ok, win, np.inf).min(axis=-1)
+                hi = np.where(ok, win, -np.inf).max(axis=-1)
+                out = np.where(nvalid > 0, hi - lo, nd_val)
+            else:  # variety: distinct valid values (NaN sorts last)
+                srt = np.sort(win, axis=-1)
+                k = np.arange(1, srt.shape[-1])
+                new = (srt[..., 1:] != srt[..., :-1]) & (k < nvalid[..., None])
+                out = np.where(nvalid > 0, 1.0 + new.sum(axis=-1), 0.0)
+    out = out.astype(np.float64)
+    if nodata is not None:
+        out[nd] = nd_val
+    return out
+
+
 def focal_mean(data: np.ndarray, radius_y: int, radius_x: int, nodata) -> np.ndarray:
     """Reference focal mean, algebra.py:3083-3101 (``_focal_mean_cpu``) via :3177-3230.
 

@@ -18,6 +18,8 @@ functions then run unmodified:
   -> ``_focal_mean_cpu``          (algebra.py:3083-3101)
 * ``raster_tri`` / ``raster_tpi`` / ``raster_curvature`` with ``use_gpu=False``
   -> ``_terrain_derivative_cpu``  (algebra.py:3352-3445)
+* ``raster_focal_min`` / ``_max`` / ``_std`` / ``_range`` / ``_variety`` with
+  ``use_gpu=False`` -> ``_focal_*_cpu``  (algebra.py:3041-3164)
 * ``raster_gaussian_filter`` / ``raster_convolve`` weight handling
   (algebra.py:2101-2154): the reference has no CPU convolution, so the
   weights it hands to ``_gpu_convolve`` are captured by replacing that one
@@ -36,6 +38,7 @@ import enum
 import json
 import sys
 import types
+import warnings
 from pathlib import Path
 
 import numpy as np
@@ -197,6 +200,8 @@ def _focal_cases() -> list[dict]:
     return cases
 
 
+FOCAL_STATS = ("min", "max", "std", "range", "variety")
+
 GAUSS_PARAMS = [(1.0, None), (1.0, 5), (0.7, None), (2.5, 8), (5.0, 41), (8.0, 65), (3.0, None)]
 
 
@@ -221,6 +226,7 @@ def main() -> None:
         "terrain": [],
         "hillshade_params": HILLSHADE_PARAMS,
         "focal_mean": [],
+        "focal_stats": list(FOCAL_STATS),
         "gaussian": [],
     }
 
@@ -263,6 +269,11 @@ def main() -> None:
         out = ref_alg.raster_focal_mean(r, c["radius"], use_gpu=False).to_numpy()
         arrays[f"focal_mean/{name}/input"] = c["data"]
         arrays[f"focal_mean/{name}/output"] = out
+        for stat in FOCAL_STATS:
+            fn = getattr(ref_alg, f"raster_focal_{stat}")
+            with warnings.catch_warnings():
+                warnings.simplefilter("ignore")
+                arrays[f"focal_{stat}/{name}/output"] = fn(r, c["radius"], use_gpu=False).to_numpy()
         manifest["focal_mean"].append(
             {
                 "name": name,

@@ -2,8 +2,8 @@
 
 The fixtures come from tests/golden/make_golden.py, which runs
 vibespatial-raster 0.1.7's ``_cpu_slope_aspect`` / ``_hillshade_cpu`` /
-``_focal_mean_cpu`` / ``_terrain_derivative_cpu`` and captures the Gaussian
-weights it builds.  CPU only.
+``_focal_mean_cpu`` / ``_focal_*_cpu`` (min, max, std, range, variety) /
+``_terrain_derivative_cpu`` and captures the Gaussian weights it builds.  CPU only.
 """
 
 from __future__ import annotations
@@ -78,6 +78,24 @@ def test_oracle_focal_mean_matches_reference(golden):
         out = oracle.focal_mean(data, ry, rx, case["nodata"])
         ref = arrays[f"focal_mean/{name}/output"]
         np.testing.assert_allclose(out, ref, rtol=1e-13, atol=1e-12, err_msg=name)
+
+
+def test_oracle_focal_statistics_match_reference(golden):
+    """min / max / range / variety bit for bit, std within 1e-13 relative
+    (summation order), against the reference's ``_focal_*_cpu``."""
+    arrays, manifest = golden
+    for case in manifest["focal_mean"]:
+        name = case["name"]
+        data = arrays[f"focal_mean/{name}/input"]
+        ry, rx = case["radius"]
+        for stat in manifest["focal_stats"]:
+            out = oracle.focal_stat(data, ry, rx, case["nodata"], stat)
+            ref = arrays[f"focal_{stat}/{name}/output"]
+            if stat == "std":
+                np.testing.assert_array_equal(np.isnan(out), np.isnan(ref), err_msg=name)
+                np.testing.assert_allclose(out, ref, rtol=1e-13, atol=0, err_msg=name)
+            else:
+                np.testing.assert_array_equal(out, ref, err_msg=f"{name} {stat}")
 
 
 def test_oracle_gaussian_weights_match_reference(golden):
