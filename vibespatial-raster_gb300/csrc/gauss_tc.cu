@@ -8,8 +8,9 @@
 // computed as a GEMM against the Toeplitz band of g:
 //   D[m][n] = sum_k A[m][k] B[k][n],  A = the tile's line windows, B[k][n] = g[k - n],
 // with the K-reversed operand layouts of the 2-D kernel (conv_tc.cu) for one
-// kernel row: A rows 16 bytes apart (LBO = 129 x 16 B between core-matrix
-// columns, SBO = 128 B), the band with SBO = LBO = 128 B.
+// kernel row: A rows 16 bytes apart (SBO = 128 B; core-matrix columns
+// 129 x 16 B apart in pass 1, 2 KB apart in pass 2), the band with
+// SBO = LBO = 128 B.
 //
 // Tile: 64 lines x 64 positions.  The MMA's M = 128 rows stack the tile's
 // numerator operand (rows 0-63) over its weight-sum operand (rows 64-127),
@@ -44,13 +45,18 @@
 // loads); the band is shifted by s = ra - r to match.
 //
 // Roles per persistent CTA (one per SM): warp 0 issues the MMAs; warp 1
-// (pass 2) copies the A windows in; warps 2-9 convert the next tile's line
-// windows into an A buffer (pass 1), then run the previous tile's epilogue
-// (tcgen05.ld, stores).  A buffers and TMEM accumulators are
-// double-buffered and handed over through mbarriers; every wait is bounded
-// (on expiry an error bit is recorded, a shared abort flag ends the other
-// roles' waits, and the MMA issuer and the copy producer wait for their
-// operations in flight before the CTA frees tensor memory).
+// (pass 2) bulk-copies the A windows in; warps 2-9 (pass 1) copy each tile's
+// raster window a tile ahead with cp.async into thread-private staging and
+// convert it into an A buffer, and run the epilogue two tiles behind the
+// conversion, so tile j-1's MMAs overlap tile j's conversion: tcgen05.ld,
+// then pass 1 stages its output chunks in shared memory for cp.async.bulk
+// stores and pass 2 exchanges numerator and weight sum through shared memory
+// and writes the quotients (its centre pixels copied a tile ahead).  A
+// buffers and TMEM accumulators are double-buffered and handed over through
+// mbarriers; every wait is bounded (on expiry an error bit is recorded, a
+// shared abort flag ends the other roles' waits, and the MMA issuer and the
+// copy producer wait for their operations in flight before the CTA frees
+// tensor memory).
 #include "tc_common.cuh"
 
 namespace vsr {
