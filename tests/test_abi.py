@@ -89,3 +89,46 @@ def test_gaussian_workspace_sizes(lib):
     # the default size from sigma (2 ceil(3 sigma) + 1 = 49) and invalid sigma
     assert lib.vsr_gaussian_workspace_bytes(100, 100, _lib.VSR_U16, 8.0, 0, _lib.VSR_PREC_AUTO) > 64 * 1024
     assert lib.vsr_gaussian_workspace_bytes(100, 100, _lib.VSR_U16, 0.0, 0, _lib.VSR_PREC_AUTO) == 0
+
+
+def _header_prototypes() -> dict[str, tuple[str, list[str]]]:
+    """name -> (return type, parameter types) of every VSR_API prototype."""
+    text = "\n".join(p.read_text() for p in sorted((ROOT / "include").glob("*.h")))
+    text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+    protos = {}
+    for ret, name, params in re.findall(r"VSR_API\s+([\w\s\*]+?)\s*\b(vsr_\w+)\s*\(([^)]*)\)\s*;", text):
+        ps = [] if params.strip() in ("", "void") else [p.strip() for p in params.split(",")]
+        # drop the parameter name, keep the type
+        types = [re.sub(r"\s+", " ", re.sub(r"\b\w+$", "", q)).strip() for q in ps]
+        protos[name] = (" ".join(ret.split()), types)
+    return protos
+
+
+def _ctype_kind(t) -> str:
+    import ctypes
+
+    if t is None:
+        return "void"
+    if t in (ctypes.c_void_p, ctypes.c_char_p) or (isinstance(t, type) and issubclass(t, ctypes._Pointer)):
+        return "ptr"
+    return {ctypes.c_int: "int", ctypes.c_int64: "int64_t", ctypes.c_double: "double", ctypes.c_uint32: "uint32_t",
+            ctypes.c_size_t: "size_t"}[t]
+
+
+def _c_kind(t: str) -> str:
+    if "*" in t:
+        return "ptr"
+    return t.replace("const ", "").strip()
+
+
+def test_ctypes_signatures_match_the_header():
+    """Argument count and kind (pointer, int, int64_t, double, uint32_t, size_t)
+    of every binding in ``_lib.SIGNATURES`` against its prototype in vsr.h."""
+    from vsr_gb300 import _lib
+
+    protos = _header_prototypes()
+    assert set(protos) == set(_lib.SIGNATURES)
+    for name, (ret, params) in protos.items():
+        restype, argtypes = _lib.SIGNATURES[name]
+        assert [_c_kind(p) for p in params] == [_ctype_kind(a) for a in argtypes], name
+        assert _c_kind(ret) == _ctype_kind(restype), name
