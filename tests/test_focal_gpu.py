@@ -58,7 +58,7 @@ def test_convolve_signed_and_zero_sum_kernels(vsr):
     for w in (np.array([[1.0, 0.0, -1.0]]), rng.uniform(-1, 1, (5, 5)), np.ones((1, 1))):
         out = vsr.raster_convolve(vsr.from_numpy(d), w, precision="fp32").to_numpy()
         ref = oracle.convolve_normalized(d, w, None)
-        # signed kernels cancel; judge against the data's magnitude
+        # signed kernels cancel: errors measured against the data's magnitude
         np.testing.assert_allclose(out, ref, rtol=1e-4, atol=1e-4 * np.abs(d).mean())
 
 
