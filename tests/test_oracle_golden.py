@@ -139,3 +139,20 @@ def test_convolve_known_answers():
     z = oracle.convolve_normalized(ones, np.array([[1.0, 0.0, -1.0]]), None)
     np.testing.assert_array_equal(z[:, :-1], 0.0)
     np.testing.assert_array_equal(z[:, -1], 1.0)
+
+
+# Known answers of the reference's own terrain-derivative tests
+# (tests/test_terrain_derivatives.py:116-139, 187-206, 255-278): 5x5 DEMs,
+# unit cells, value at the centre pixel.
+TERRAIN_KNOWN_ANSWERS = [
+    ("tri", np.add.outer(np.arange(5.0), np.arange(1.0, 6.0)), 1.0),
+    ("tpi", np.where(np.add.outer(np.abs(np.arange(5) - 2), np.abs(np.arange(5) - 2)) == 0, 10.0, 1.0), 9.0),
+    ("curvature", np.array([[0, 0, 0, 0, 0], [0, 0, 1, 0, 0], [0, 1, 4, 1, 0], [0, 0, 1, 0, 0], [0, 0, 0, 0, 0]],
+                           np.float64), 1200.0),
+]
+
+
+@pytest.mark.parametrize("kind,data,centre", TERRAIN_KNOWN_ANSWERS)
+def test_oracle_terrain_known_answers(kind, data, centre):
+    out, nd = oracle.terrain_derivative(data, (1.0, 0.0, 0.0, 0.0, -1.0, 5.0), None, kind)
+    assert out[2, 2] == centre and nd == -9999.0 and out[0, 0] == nd

@@ -118,3 +118,18 @@ def test_api_contract(vsr):
     assert (tri.to_numpy()[0] == -9999.0).all()
     with pytest.raises(NotImplementedError):
         vsr.raster_tri(r, use_gpu=False)
+
+
+@pytest.mark.parametrize("kind,data,centre", [
+    ("tri", np.add.outer(np.arange(5.0), np.arange(1.0, 6.0)), 1.0),
+    ("tpi", np.where(np.add.outer(np.abs(np.arange(5) - 2), np.abs(np.arange(5) - 2)) == 0, 10.0, 1.0), 9.0),
+    ("curvature", np.array([[0, 0, 0, 0, 0], [0, 0, 1, 0, 0], [0, 1, 4, 1, 0], [0, 0, 1, 0, 0], [0, 0, 0, 0, 0]],
+                           np.float64), 1200.0),
+])
+def test_reference_known_answers(vsr, kind, data, centre):
+    """Reference tests/test_terrain_derivatives.py:116-139, 187-206, 255-278
+    (float64 DEMs, unit cells), and the same DEMs as float32."""
+    for dt in (np.float64, np.float32):
+        r = vsr.from_numpy(data.astype(dt), affine=(1.0, 0.0, 0.0, 0.0, -1.0, 5.0))
+        out = vsr.raster_terrain_derivatives(r)[kind].to_numpy()
+        assert out[2, 2] == centre and out[0, 0] == -9999.0
