@@ -167,19 +167,21 @@ VSR_API int vsr_convolve(const void* src, int dtype, int64_t height, int64_t wid
 
 /* ---- normalised focal convolution that allocates nothing -----------------
  * No counterpart in the reference.  For callers that cannot allocate device
- * memory and cannot pass a workspace: a serving process whose device budget
- * was fixed at start-up, a host that reaches this library through a plugin
- * boundary (ctypes / cgo / JNI) without the process allocator, or work issued
- * while a CUDA graph capture forbids allocation.  Same arguments and results
- * as vsr_convolve without the workspace: the scratch is a static device
- * array inside libvsr (248,320 bytes, enough for kernels up to 80 x 80,
- * held by every GPU that loads the library until the process exits).
- * Kernels larger than 80 x 80 are rejected with VSR_ERR_UNSUPPORTED.  The
- * first call on each device resolves the array's device address (with that
- * device current), so make it before any stream capture.  All calls share
- * the array and it keeps the last call's contents; calls whose kernels
- * overlap on the GPU (e.g. on two streams at once) race.  No cudaMalloc,
- * cudaFree or allocating library routine is called. */
+ * memory and cannot pass a workspace: a serving process whose device memory
+ * budget was fixed when it started, or a host that reaches this library
+ * through a plugin boundary (ctypes / cgo / JNI) with no access to the
+ * process's device allocator.  Same arguments and results as vsr_convolve
+ * without the workspace: the scratch is a static device array inside libvsr
+ * (248,320 bytes, enough for every kernel up to 80 x 80 at any precision;
+ * every GPU that loads the library holds it until the process exits).
+ * Larger kernels are rejected with VSR_ERR_UNSUPPORTED.  The first call on
+ * each device resolves the array's device address (with that device
+ * current); make that first call before any stream capture.  All calls share
+ * the one array and it keeps the last call's contents (each call rewrites
+ * every scratch byte it reads); calls whose kernels overlap on the GPU (e.g.
+ * on two streams at once) race on it.  No cudaMalloc, cudaFree or allocating
+ * library routine is called.  ``weights_host`` is staged into the scratch
+ * with cudaMemcpyAsync on ``stream``, as in vsr_convolve. */
 VSR_API int vsr_convolve_noalloc(const void* src, int dtype, int64_t height, int64_t width, int64_t pitch,
                          const double* weights_host, int kh, int kw, double nodata, int nodata_kind,
                          void* dst, int out_dtype, int64_t out_pitch, int precision, void* stream);
@@ -253,8 +255,10 @@ VSR_API int vsr_focal_mean_bands(const void* src, int dtype, int bands, int64_t 
  * work counter and launches; it makes no host synchronisation and no
  * allocation, so it can be captured in a CUDA graph and replayed.  The plan
  * keeps the tile pointers: replays read and write the same buffers.  The
- * block shape comes from the tuning table (VSR_OP_BATCH); re-plan after
- * changing it. */
+ * block shape is the tuning table's (VSR_OP_BATCH) when the plan is built;
+ * vsr_batch_run launches the plan's own shape whatever the table holds later
+ * (re-plan to adopt a new choice), and rejects a ``gauss_k`` other than the
+ * plan's, or a plan that vsr_batch_plan did not build in this process. */
 typedef struct vsr_batch_tile {
   const float* src;           /* height x width float32, row pitch ``pitch`` */
   int64_t height, width, pitch;

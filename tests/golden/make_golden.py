@@ -2,7 +2,7 @@
 
 Run in a container where the reference source tree is present:
 
-    python tests/golden/make_golden.py [--reference /root/reference]
+    python tests/golden/make_golden.py --reference <path to the reference source tree>
 
 The reference package (vibespatial-raster 0.1.7) imports two modules from its
 external core runtime (``vibespatial.residency`` and ``vibespatial.runtime``)
@@ -207,7 +207,7 @@ GAUSS_PARAMS = [(1.0, None), (1.0, 5), (0.7, None), (2.5, 8), (5.0, 41), (8.0, 6
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True, help="root of the reference source tree (holds src/vibespatial)")
     ap.add_argument("--out", default=str(HERE / "focal_golden.npz"))
     args = ap.parse_args()
 

@@ -115,3 +115,36 @@ def test_batch_rejects_bad_plans(vsr):
     r = vsr.from_numpy(np.zeros((8, 8), np.float32))
     with pytest.raises(NotImplementedError):
         batch.TerrainBatch([r], sigma=3.0, kernel_size=19)
+
+
+def test_batch_run_keeps_the_plans_shape(vsr):
+    """A tuning change between plan and run does not change what the run writes."""
+    import ctypes
+
+    import torch
+
+    from vsr_gb300 import _lib, batch
+
+    lib = _lib.load()
+    rasters = _tiles(vsr, n=5, seed=2)
+    _lib.check(lib.vsr_tuning_set(_lib.VSR_OP_BATCH, 2), "set")  # 16-row blocks
+    b = batch.TerrainBatch(rasters, sigma=1.0, kernel_size=5)
+    b.run()
+    ref = [{k: v.to_numpy().copy() for k, v in d.items()} for d in b.results()]
+    for (s, a, g) in b.outputs:
+        s.fill_(0)
+        a.fill_(0)
+        g.fill_(0)
+    _lib.check(lib.vsr_tuning_set(_lib.VSR_OP_BATCH, 1), "set")  # 64-row blocks, not re-planned
+    b.run()
+    torch.cuda.synchronize()
+    for d0, d in zip(ref, b.results()):
+        for k in d0:
+            np.testing.assert_array_equal(d[k].to_numpy(), d0[k])
+    code = ctypes.c_uint32(0)
+    _lib.check(lib.vsr_poll_device_error(None, ctypes.byref(code)), "poll")
+    assert code.value == 0
+    # a Gaussian width other than the plan's is refused on the host
+    st = lib.vsr_batch_run(b.plan, 3, torch.cuda.current_stream().cuda_stream)
+    assert st == _lib.VSR_ERR_INVALID_ARG and "does not match" in _lib.last_error()
+    _lib.check(lib.vsr_tuning_set(_lib.VSR_OP_BATCH, 0), "set")

@@ -14,8 +14,8 @@
 //    128 bytes every (n-group, k-chunk) pair maps to core matrix n/8 + k/8,
 //    so one kernel row's Toeplitz band is Kp/8 + 64/8 - 1 core matrices.
 // Tile width: a tcgen05.mma with M = 128 costs a fixed ~51 cycles up to
-// N = 64 and runs at the full rate only from N = 128
-// (diagnostics/mma_issue_probe.cu); with the Toeplitz padding (N + kw - 1
+// N = 64 and runs at the full rate only from N = 128 (measured on GB300 with
+// a one-thread loop of dependent MMAs); with the Toeplitz padding (N + kw - 1
 // taps of K per N outputs) N = 64 and N = 128 cost the same per output and
 // N = 64 needs half the shared memory.
 //

@@ -3,15 +3,14 @@
 //
 // Some callers of this library cannot call cudaMalloc, and cannot hand us a
 // workspace either: a serving process whose device memory budget was fixed
-// when it started, a host that reaches this library through a plugin
-// boundary (ctypes / cgo / JNI) without access to the process allocator, or
-// code that issues work while a CUDA graph is captured in a mode that
-// forbids allocation.  For them this entry point takes only the inputs and
-// the output; its scratch (the staged float64 weights and the float32 or
-// BF16 operand images built from them) lives in a file-scope __device__ array sized
-// for the largest supported kernel of either precision.  Every GPU that
-// loads the library holds that array (kNoAllocScratchBytes, 242.5 KiB)
-// until the process exits.
+// when it started, or a host that reaches this library through a plugin
+// boundary (ctypes / cgo / JNI) with no access to the process's device
+// allocator.  For them this entry point takes only the inputs and the output;
+// its scratch (the staged float64 weights and the float32 or BF16 operand
+// images built from them) lives in a file-scope __device__ array sized for the
+// largest supported kernel of either precision.  Every GPU that loads the
+// library holds that array (kNoAllocScratchBytes, 242.5 KiB) until the process
+// exits.
 //
 // Host code cannot use the array's name as a device address, so on the first
 // call on each device (with that device current) the address is resolved
@@ -25,8 +24,6 @@
 #include "vsr_internal.cuh"
 
 namespace vsr {
-
-size_t conv_ws_plain(int kh, int kw);  // focal.cu
 
 namespace {
 
@@ -74,7 +71,10 @@ extern "C" int vsr_convolve_noalloc(const void* src, int dtype, int64_t height, 
   if (kh > kNoAllocMaxK || kw > kNoAllocMaxK)
     return fail(VSR_ERR_UNSUPPORTED, "vsr_convolve_noalloc: kernel %dx%d exceeds the %dx%d maximum of its static scratch",
                 kh, kw, kNoAllocMaxK, kNoAllocMaxK);
-  if (kh > 0 && kw > 0 && conv_ws_plain(kh, kw) > kNoAllocScratchBytes)
+  // Whatever path vsr_convolve takes for this kernel and precision (the FP32
+  // kernels, or the tensor-core path that AUTO may pick), its workspace must
+  // fit the static array.
+  if (kh > 0 && kw > 0 && vsr_convolve_workspace_size(kh, kw, precision) > kNoAllocScratchBytes)
     return fail(VSR_ERR_UNSUPPORTED, "vsr_convolve_noalloc: kernel %dx%d needs more than %zu scratch bytes", kh, kw,
                 kNoAllocScratchBytes);
   void* ws = scratch_for_current_device();

@@ -29,7 +29,9 @@
 //    hillshade stores.
 //  * horn_generic  -- every other dtype / alignment: one thread per pixel,
 //    clamped loads through L1.
+#include <mutex>
 #include <type_traits>
+#include <unordered_map>
 #include <vector>
 
 #include "vsr_internal.cuh"
@@ -946,8 +948,16 @@ constexpr int kBatchSmemTiles = 2048;  // tiles whose prefix sums are searched i
 
 template <int TH, int THREADS, int KG>
 __global__ void __launch_bounds__(THREADS) batch_terrain_kernel(BatchHeader* __restrict__ hdr,
-                                                                const BatchTileDev* __restrict__ tiles) {
+                                                                const BatchTileDev* __restrict__ tiles,
+                                                                uint32_t* err_word) {
   using L = BatchSmem<TH, THREADS, KG>;
+  // The plan's item counts were formed with its own block height and its taps
+  // with its own Gaussian width: a launch of any other shape would leave rows
+  // unwritten or apply the wrong taps, so it reports and does nothing.
+  if (hdr->th != TH || (hdr->kg > 1 ? hdr->kg : 1) != KG) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err_word, kDevErrPlan);
+    return;
+  }
   constexpr int WARPS = THREADS / 32;
   constexpr int RB = TH / WARPS;
   constexpr int HY = L::HY, SR = L::SR;
@@ -1156,13 +1166,15 @@ constexpr int kNumBatchConfigs = sizeof(kBatchConfigs) / sizeof(kBatchConfigs[0]
 template <int TH, int THREADS, int KG>
 int launch_batch_t(BatchHeader* hdr, const BatchTileDev* tiles, cudaStream_t st) {
   using L = BatchSmem<TH, THREADS, KG>;
+  uint32_t* err = device_error_word();
+  if (!err) return VSR_ERR_CUDA;
   const size_t smem = static_cast<size_t>(L::kFloats) * 4;
   auto kern = batch_terrain_kernel<TH, THREADS, KG>;
   VSR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   int per_sm = 0;
   VSR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, THREADS, smem));
   if (per_sm < 1) return fail(VSR_ERR_CUDA, "batch kernel cannot be resident");
-  kern<<<static_cast<unsigned>(sm_count() * per_sm), THREADS, smem, st>>>(hdr, tiles);
+  kern<<<static_cast<unsigned>(sm_count() * per_sm), THREADS, smem, st>>>(hdr, tiles, err);
   VSR_CUDA_TRY(cudaGetLastError());
   return VSR_OK;
 }
@@ -1197,6 +1209,15 @@ __global__ void prep_batch_gauss(BatchHeader* hdr, int kg, double sigma) {
   }
   hdr->gsum = static_cast<float>(s);
 }
+
+// Launch shape of every plan built in this process, keyed by the plan's
+// device address: vsr_batch_run launches the configuration the plan was
+// built for, whatever the tuning table holds by then.
+struct PlanShape {
+  int cfg, kg;
+};
+std::mutex g_plan_mutex;
+std::unordered_map<const void*, PlanShape> g_plans;
 
 }  // namespace
 
@@ -1275,6 +1296,10 @@ extern "C" int vsr_batch_plan(const vsr_batch_tile* tiles_host, int n_tiles, dou
     VSR_CUDA_TRY(cudaGetLastError());
   }
   VSR_CUDA_TRY(cudaStreamSynchronize(st));  // the host descriptors are staged from pageable memory
+  {
+    std::lock_guard<std::mutex> lk(g_plan_mutex);
+    g_plans[plan] = PlanShape{cfg, gauss_k};
+  }
   if (total_items) *total_items = items;
   return VSR_OK;
 }
@@ -1285,8 +1310,18 @@ extern "C" int vsr_batch_run(void* plan, int gauss_k, void* stream) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   BatchHeader* hdr = static_cast<BatchHeader*>(plan);
   const BatchTileDev* tiles = reinterpret_cast<const BatchTileDev*>(static_cast<char*>(plan) + ((sizeof(BatchHeader) + 255) & ~size_t(255)));
+  PlanShape shape{};
+  {
+    std::lock_guard<std::mutex> lk(g_plan_mutex);
+    const auto it = g_plans.find(plan);
+    if (it == g_plans.end())
+      return fail(VSR_ERR_INVALID_ARG, "plan %p was not built by vsr_batch_plan in this process", plan);
+    shape = it->second;
+  }
+  if (gauss_k != shape.kg)
+    return fail(VSR_ERR_INVALID_ARG, "gauss_k %d does not match the plan's %d", gauss_k, shape.kg);
   VSR_CUDA_TRY(cudaMemsetAsync(&hdr->counter, 0, sizeof(hdr->counter), st));
-  const int cfg = tuning_get(VSR_OP_BATCH);
+  const int cfg = shape.cfg;
   switch (gauss_k) {
     case 0:
     case 1: return launch_batch_kg<1>(cfg, hdr, tiles, st);

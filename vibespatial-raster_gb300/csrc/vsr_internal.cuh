@@ -34,6 +34,7 @@ enum DeviceError : uint32_t {
   kDevErrTmaTimeout = 1u,
   kDevErrMmaTimeout = 2u,
   kDevErrQueue = 4u,
+  kDevErrPlan = 8u,  // a batch launch whose shape differs from its plan's
 };
 uint32_t* device_error_word();  // nullptr (and error set) on failure
 

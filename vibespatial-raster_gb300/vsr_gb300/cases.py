@@ -13,6 +13,10 @@ It is the small, single-kernel command to run under a profiler:
     gaussian    the same uint16 stack, Gaussian sigma / kernel size
                 (--precision split_bf16: the tensor-core line passes;
                 fp32: the separable CUDA-core kernels)
+    horn        fused slope + aspect + hillshade on the fBm DEM with 200
+                -9999 disc holes (the 16384^2 terrain workload at a chosen
+                size), one launch configuration of the Horn kernel
+                (--config, an index into the tuning table)
 
 Run with ``PYTHONPATH=vibespatial-raster_gb300`` from the repository root.
 """
@@ -53,7 +57,7 @@ def _uint16_stack(bands: int, size: int):
 
 def main(argv=None) -> None:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
-    ap.add_argument("op", choices=["conv", "focal_mean", "gaussian"])
+    ap.add_argument("op", choices=["conv", "focal_mean", "gaussian", "horn"])
     ap.add_argument("--size", type=int, default=None, help="raster side (default: 4096 conv, 10980 others)")
     ap.add_argument("--bands", type=int, default=1)
     ap.add_argument("--k", type=int, default=31, help="kernel side (conv, gaussian)")
@@ -61,6 +65,7 @@ def main(argv=None) -> None:
     ap.add_argument("--radius", type=int, default=3)
     ap.add_argument("--precision", default="split_bf16", choices=["auto", "fp32", "split_bf16"])
     ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--config", type=int, default=0, help="Horn launch configuration (horn)")
     args = ap.parse_args(argv)
 
     import torch
@@ -77,6 +82,19 @@ def main(argv=None) -> None:
         out = torch.empty((1, n, n), dtype=torch.float32, device=dev)
         ms = _timed(lambda: algebra.convolve_bands(r, w, precision=args.precision, out_dtype=np.float32, out=out),
                     args.reps)
+        px = n * n
+    elif args.op == "horn":
+        from vsr_gb300 import _lib
+
+        n = args.size or 8192
+        dem = workloads.terrain_16k(device=dev, size=n)
+        r = vsr.from_device(dem.data, nodata=dem.nodata, affine=dem.affine)
+        lib = _lib.load()
+        _lib.check(lib.vsr_tuning_set(_lib.VSR_OP_HORN, args.config), "vsr_tuning_set")
+        outs = (torch.empty((1, n, n), dtype=torch.float32, device=dev),
+                torch.empty((1, n, n), dtype=torch.float32, device=dev),
+                torch.empty((1, n, n), dtype=torch.uint8, device=dev))
+        ms = _timed(lambda: algebra.horn_fused(r, out=outs), args.reps)
         px = n * n
     else:
         n = args.size or 10980
