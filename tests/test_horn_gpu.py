@@ -223,8 +223,8 @@ def test_terrain_16k_strips_vs_oracle(vsr):
 
 @pytest.mark.parametrize("shape", [(300, 1000), (517, 1024), (64, 128)])
 def test_every_launch_config_gives_identical_results(vsr, shape):
-    """All autotuner configurations -- direct stores and TMA tensor stores,
-    every tile height -- write bit-identical outputs, on rasters whose edges
+    """All autotuner configurations -- every tile height, thread count and
+    register budget -- write bit-identical outputs, on rasters whose edges
     cut tiles and with nodata present."""
     from vsr_gb300 import _lib
 
@@ -234,7 +234,7 @@ def test_every_launch_config_gives_identical_results(vsr, shape):
     r = vsr.from_numpy(z, nodata=-9999.0, affine=(10.0, 0, 0, 0, -10.0, 0))
     lib = _lib.load()
     n = lib.vsr_tuning_count(_lib.VSR_OP_HORN)
-    assert n >= 7
+    assert n >= 5
     ref = None
     try:
         for cfg in range(n):

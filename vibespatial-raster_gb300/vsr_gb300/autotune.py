@@ -2,7 +2,7 @@
 
 libvsr keeps, per tunable operation, a small table of launch configurations
 (for the fused Horn kernel: output rows per tile, TMA pipeline stages,
-threads per CTA and the shared-memory output tiles of TMA stores).  ``autotune_horn`` times every configuration on the
+threads per CTA and the CTAs per SM its register budget is sized for).  ``autotune_horn`` times every configuration on the
 caller's own raster with CUDA events, selects the fastest through
 ``vsr_tuning_set`` and records the choice in an on-disk cache keyed by
 (operation, raster size class, dtype, SM count) so later processes apply it
@@ -19,9 +19,8 @@ from pathlib import Path
 from vsr_gb300 import _lib
 
 HORN_CONFIGS = [  # mirrors kHornConfigs in csrc/horn.cu:
-    # (rows per tile, stages, threads, TMA-store tiles, CTAs per SM the registers are sized for)
-    (64, 2, 128, 0, 4), (32, 2, 128, 0, 4), (32, 2, 128, 0, 5), (32, 2, 128, 0, 6), (64, 2, 256, 0, 3),
-    (32, 3, 128, 0, 4), (32, 2, 256, 2, 3), (16, 2, 256, 2, 3),
+    # (rows per tile, TMA stages, threads per CTA, CTAs per SM the registers are sized for)
+    (64, 2, 128, 4), (48, 2, 128, 4), (32, 2, 128, 4), (32, 2, 128, 5), (64, 2, 256, 2),
 ]
 
 

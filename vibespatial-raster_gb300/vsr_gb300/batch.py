@@ -156,6 +156,33 @@ def per_tile_launches(rasters: list[OwnedRasterArray], *, sigma: float = 1.0, ke
     return res
 
 
+class PerTileGraph:
+    """The unbatched comparison in its fastest form: one Horn launch and one
+    Gaussian call per tile (``per_tile_launches``), recorded once into a CUDA
+    graph and replayed, so that a replay costs the kernels and not Python."""
+
+    def __init__(self, rasters: list[OwnedRasterArray], *, sigma: float = 1.0, kernel_size: int = 5):
+        import torch
+
+        self.rasters = rasters
+        self.outs = []
+        for r in rasters:
+            t = r.device_data()
+            H, W = t.shape[-2:]
+            self.outs.append(tuple(torch.empty((1, H, W), dtype=torch.float32, device=t.device) for _ in range(3)))
+        self.sigma, self.k = sigma, kernel_size
+        per_tile_launches(rasters, sigma=sigma, kernel_size=kernel_size, outs=self.outs)  # warm-up outside capture
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            per_tile_launches(rasters, sigma=sigma, kernel_size=kernel_size, outs=self.outs)
+        # per tile: the Horn kernel, the Gaussian tap build and the separable Gaussian
+        self.launches = 3 * len(rasters)
+
+    def replay(self):
+        self.graph.replay()
+
+
 def autotune_batch(batch: TerrainBatch, *, repeats: int = 3) -> dict:
     """Time every batch launch configuration on ``batch`` and keep the fastest."""
     import torch
@@ -185,6 +212,6 @@ def autotune_batch(batch: TerrainBatch, *, repeats: int = 3) -> dict:
 
 BATCH_CONFIGS = [(32, 256), (64, 256), (16, 128), (32, 128)]  # kBatchConfigs: (rows per block, threads)
 
-__all__ = ["TerrainBatch", "per_tile_launches", "autotune_batch", "BATCH_CONFIGS"]
+__all__ = ["TerrainBatch", "PerTileGraph", "per_tile_launches", "autotune_batch", "BATCH_CONFIGS"]
 
 

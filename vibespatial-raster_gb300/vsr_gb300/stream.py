@@ -37,8 +37,14 @@ def _pinned_view(a: np.ndarray):
 def terrain_host(dem: np.ndarray, affine, nodata, *, slope_out: np.ndarray | None = None,
                  aspect_out: np.ndarray | None = None, hs_out: np.ndarray | None = None,
                  azimuth: float = 315.0, altitude: float = 45.0, z_factor: float = 1.0,
-                 nodata_mode: str = NODATA_WINDOW, strip_rows: int = 1024, n_streams: int = 3):
-    """Fill the given host arrays (float32 slope/aspect, uint8 hillshade) from a host DEM."""
+                 nodata_mode: str = NODATA_WINDOW, strip_rows: int = 1024, n_streams: int = 3,
+                 phase_events: list | None = None):
+    """Fill the given host arrays (float32 slope/aspect, uint8 hillshade) from a host DEM.
+
+    ``phase_events``: a list that receives, per strip, four CUDA events
+    recorded on the strip's stream before its host->device copy, after it,
+    after the kernel and after its device->host copies (see phase_summary).
+    """
     import torch
 
     if dem.ndim != 2 or dem.dtype != np.float32:
@@ -83,27 +89,52 @@ def terrain_host(dem: np.ndarray, affine, nodata, *, slope_out: np.ndarray | Non
         rows = hi - lo
         s = streams[i % n_streams]
         d_in, d_s, d_a, d_h = bufs[i % n_streams]
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)] if phase_events is not None else None
         with torch.cuda.stream(s):
+            if ev:
+                ev[0].record(s)
             d_in[:rows].copy_(src_t[lo:hi], non_blocking=True)
+            if ev:
+                ev[1].record(s)
             st = lib.vsr_horn_fused(
                 d_in.data_ptr(), _lib.VSR_F32, rows, W, W, cx, cy, ndv, kind, flags,
                 d_s.data_ptr() if d_s is not None else None, d_a.data_ptr() if d_a is not None else None,
                 _lib.VSR_F32, W, d_h.data_ptr() if d_h is not None else None, W, float(z_factor), zen, az,
                 s.cuda_stream)
             _lib.check(st, "vsr_horn_fused")
+            if ev:
+                ev[2].record(s)
             a, b = y0 - lo, y1 - lo  # inner rows of the strip
             for d, h in zip((d_s, d_a, d_h), host_outs):
                 if d is not None:
                     h[y0:y1].copy_(d[a:b], non_blocking=True)
+            if ev:
+                ev[3].record(s)
+                phase_events.append(ev)
     for s in streams:
         cur.wait_stream(s)
     cur.synchronize()
 
 
+def phase_summary(phase_events: list) -> dict:
+    """Per-phase device time of a streamed pass from terrain_host's events:
+    the summed host->device, kernel and device->host times over the strips,
+    and the span from the first strip's start to the last strip's end (the
+    phases of different strips overlap, so the sums exceed the span)."""
+    if not phase_events:
+        return {}
+    h2d = sum(e[0].elapsed_time(e[1]) for e in phase_events)
+    ker = sum(e[1].elapsed_time(e[2]) for e in phase_events)
+    d2h = sum(e[2].elapsed_time(e[3]) for e in phase_events)
+    first = phase_events[0][0]
+    span = max(first.elapsed_time(e[3]) for e in phase_events)
+    return {"strips": len(phase_events), "h2d_ms": h2d, "kernel_ms": ker, "d2h_ms": d2h, "span_ms": span}
+
+
 def raster_terrain_host(dem: OwnedRasterArray, *, slope: bool = True, aspect: bool = True, hillshade: bool = True,
                         azimuth: float = 315.0, altitude: float = 45.0, z_factor: float = 1.0,
                         nodata_mode: str = NODATA_WINDOW, out=None, strip_rows: int = 1024,
-                        n_streams: int = 3) -> dict[str, OwnedRasterArray]:
+                        n_streams: int = 3, phase_events: list | None = None) -> dict[str, OwnedRasterArray]:
     """``raster_terrain`` for a host-resident DEM with host-resident results.
 
     Streams row strips through the GPU (copies overlapped with the fused
@@ -128,7 +159,7 @@ def raster_terrain_host(dem: OwnedRasterArray, *, slope: bool = True, aspect: bo
     terrain_host(np.asarray(z, dtype=np.float32), dem.affine, dem.nodata, slope_out=o_s if slope else None,
                  aspect_out=o_a if aspect else None, hs_out=o_h if hillshade else None, azimuth=azimuth,
                  altitude=altitude, z_factor=z_factor, nodata_mode=nodata_mode, strip_rows=strip_rows,
-                 n_streams=n_streams)
+                 n_streams=n_streams, phase_events=phase_events)
     res = {}
     if slope:
         res["slope"] = from_numpy(o_s, nodata=dem.nodata, affine=dem.affine, crs=dem.crs)
