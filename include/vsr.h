@@ -80,8 +80,25 @@ VSR_API const char* vsr_last_error(void);      /* message of this thread's last 
 /* SM count and compute capability of the current device (cudaGetDevice). */
 VSR_API int vsr_device_info(int* sm_count, int* cc_major, int* cc_minor);
 /* Synchronise ``stream``, then read and clear the device-side error word that
- * kernels set when a bounded wait ran out (0 = none).  Synchronises. */
+ * kernels set when a bounded wait ran out (0 = none; else an OR of the
+ * VSR_DEVERR_* bits below).  Synchronises.  Every spin-wait in a libvsr
+ * kernel (on an mbarrier phase that a TMA copy or a tensor-core commit
+ * completes) gives up after 2 s, sets its bit, gives the copies it issued a
+ * bounded time to land and returns, so the context stays usable. */
+#define VSR_DEVERR_TMA_TIMEOUT 1u /* a TMA / cp.async stage never arrived      */
+#define VSR_DEVERR_MMA_TIMEOUT 2u /* a tcgen05 commit or TMEM stage never came */
+#define VSR_DEVERR_QUEUE 4u       /* a batch work item was out of range        */
+#define VSR_DEVERR_PLAN 8u        /* a batch launch disagreed with its plan    */
 VSR_API int vsr_poll_device_error(void* stream, uint32_t* code);
+/* Exercise the bounded-wait path: one CTA initialises an mbarrier that no
+ * copy or thread will ever complete and waits on it with the same bounded
+ * wait the kernels use, with a limit of ``limit_ns`` (1e3 .. 2e9 ns) in place
+ * of the usual 2 s.  The wait runs out, VSR_DEVERR_TMA_TIMEOUT is raised in
+ * the device error word (read it with vsr_poll_device_error) and the kernel
+ * writes result[0] = 1 (the wait gave up) and result[1] = the nanoseconds it
+ * waited, capped at 2^32 - 1 (``result``: two device uint32 words).  Nothing
+ * is in flight when it returns.  No counterpart in the reference. */
+VSR_API int vsr_wait_selftest(uint64_t limit_ns, uint32_t* result, void* stream);
 
 /* ---- launch-configuration tuning ----------------------------------------
  * Tunable operations have a small table of launch configurations (tile
@@ -123,6 +140,17 @@ VSR_API int vsr_horn_fused(const void* dem, int dtype, int64_t height, int64_t w
                    uint8_t* hillshade, int64_t hs_pitch, double z_factor, double zenith_rad,
                    double azimuth_rad, void* stream);
 
+/* Band-first stacks in ONE launch: ``bands`` DEMs ``band_stride`` elements
+ * apart; slope/aspect bands ``out_band_stride`` and hillshade bands
+ * ``hs_band_stride`` elements apart; otherwise as vsr_horn_fused.  Replaces
+ * the per-band loop of dispatch_per_band_gpu (dispatch.py:417-506). */
+VSR_API int vsr_horn_fused_bands(const void* dem, int dtype, int bands, int64_t band_stride, int64_t height,
+                                 int64_t width, int64_t pitch, double cell_x, double cell_y, double nodata,
+                                 int nodata_kind, uint32_t flags, void* slope, void* aspect, int out_dtype,
+                                 int64_t out_band_stride, int64_t out_pitch, uint8_t* hillshade,
+                                 int64_t hs_band_stride, int64_t hs_pitch, double z_factor, double zenith_rad,
+                                 double azimuth_rad, void* stream);
+
 /* ---- terrain derivatives: TRI, TPI, profile curvature -------------------
  * Replaces the ``terrain_derivatives`` launches (algebra.py:2854-2991, kernel
  * kernels/focal.py:487-647), one per derivative, with one pass for any subset,
@@ -141,6 +169,12 @@ VSR_API int vsr_terrain_derivatives(const void* dem, int dtype, int64_t height, 
                                     double cell_x, double cell_y, double nodata, int nodata_kind,
                                     double nodata_out, void* tri, void* tpi, void* curvature, int out_dtype,
                                     int64_t out_pitch, void* stream);
+
+/* Band-first stacks in one launch (see vsr_horn_fused_bands). */
+VSR_API int vsr_terrain_derivatives_bands(const void* dem, int dtype, int bands, int64_t band_stride, int64_t height,
+                                          int64_t width, int64_t pitch, double cell_x, double cell_y, double nodata,
+                                          int nodata_kind, double nodata_out, void* tri, void* tpi, void* curvature,
+                                          int out_dtype, int64_t out_band_stride, int64_t out_pitch, void* stream);
 
 /* ---- nodata-aware normalised focal convolution --------------------------
  * Replaces the ``convolve_normalized`` launch (algebra.py:2077-2083, kernel
@@ -164,6 +198,14 @@ VSR_API int vsr_convolve(const void* src, int dtype, int64_t height, int64_t wid
                  const double* weights_host, int kh, int kw, double nodata, int nodata_kind,
                  void* dst, int out_dtype, int64_t out_pitch, int precision, void* workspace,
                  size_t workspace_bytes, void* stream);
+
+/* Band-first stacks in one launch (see vsr_horn_fused_bands); the workspace
+ * is the same as for one band. */
+VSR_API int vsr_convolve_bands(const void* src, int dtype, int bands, int64_t band_stride, int64_t height,
+                               int64_t width, int64_t pitch, const double* weights_host, int kh, int kw,
+                               double nodata, int nodata_kind, void* dst, int out_dtype, int64_t out_band_stride,
+                               int64_t out_pitch, int precision, void* workspace, size_t workspace_bytes,
+                               void* stream);
 
 /* ---- normalised focal convolution that allocates nothing -----------------
  * No counterpart in the reference.  For callers that cannot allocate device
@@ -241,6 +283,39 @@ VSR_API int vsr_focal_mean_bands(const void* src, int dtype, int bands, int64_t 
                          int64_t width, int64_t pitch, int radius_y, int radius_x, double nodata,
                          int nodata_kind, void* dst, int out_dtype, int64_t out_band_stride, int64_t out_pitch,
                          void* stream);
+
+/* ---- focal statistics ------------------------------------------------------
+ * Replaces the ``focal_stats`` launch (algebra.py:3239-3349, kernel
+ * kernels/focal.py:666-770) for every statistic, with the reference CPU
+ * functions' semantics (algebra.py:3041-3164, pinned by the oracle):
+ *   VSR_STAT_MIN / _MAX  nodata taps excluded, and every tap equal to the
+ *                        +inf / -inf placeholder with them (valid +-inf data
+ *                        too); a NaN tap gives NaN;
+ *   VSR_STAT_MEAN        as vsr_focal_mean;
+ *   VSR_STAT_STD         population standard deviation of the valid
+ *                        (non-nodata, non-NaN) taps, 0.0 for an empty window;
+ *                        exact integer sums for 8/16-bit rasters, two passes
+ *                        in float64 otherwise;
+ *   VSR_STAT_RANGE       max - min of the valid taps;
+ *   VSR_STAT_VARIETY     number of distinct valid values, 0 for an empty
+ *                        window (no cap; the reference GPU kernel stops at 49).
+ * Out-of-bounds taps are excluded.  An empty window gives ``nodata`` (0.0
+ * when nodata_kind is VSR_NODATA_NONE); a nodata centre gives ``nodata``.
+ * Radii up to 31 (variety: 7); larger ones return VSR_ERR_UNSUPPORTED. */
+#define VSR_STAT_MIN 0
+#define VSR_STAT_MAX 1
+#define VSR_STAT_MEAN 2
+#define VSR_STAT_STD 3
+#define VSR_STAT_RANGE 4
+#define VSR_STAT_VARIETY 5
+VSR_API int vsr_focal_stat(const void* src, int dtype, int64_t height, int64_t width, int64_t pitch, int stat,
+                           int radius_y, int radius_x, double nodata, int nodata_kind, void* dst, int out_dtype,
+                           int64_t out_pitch, void* stream);
+/* Band-first stacks in one launch (see vsr_gaussian_bands). */
+VSR_API int vsr_focal_stat_bands(const void* src, int dtype, int bands, int64_t band_stride, int64_t height,
+                                 int64_t width, int64_t pitch, int stat, int radius_y, int radius_x, double nodata,
+                                 int nodata_kind, void* dst, int out_dtype, int64_t out_band_stride,
+                                 int64_t out_pitch, void* stream);
 
 /* ---- batched tiles: one persistent launch ------------------------------------
  * Many float32 DEM tiles of uneven sizes, each with its own cell size and

@@ -111,18 +111,20 @@ def _ctype_kind(t) -> str:
         return "void"
     if t in (ctypes.c_void_p, ctypes.c_char_p) or (isinstance(t, type) and issubclass(t, ctypes._Pointer)):
         return "ptr"
+    # c_size_t and c_uint64 are the same ctypes type on LP64 targets
     return {ctypes.c_int: "int", ctypes.c_int64: "int64_t", ctypes.c_double: "double", ctypes.c_uint32: "uint32_t",
-            ctypes.c_size_t: "size_t"}[t]
+            ctypes.c_size_t: "u64"}[t]
 
 
 def _c_kind(t: str) -> str:
     if "*" in t:
         return "ptr"
-    return t.replace("const ", "").strip()
+    t = t.replace("const ", "").strip()
+    return "u64" if t in ("size_t", "uint64_t") else t
 
 
 def test_ctypes_signatures_match_the_header():
-    """Argument count and kind (pointer, int, int64_t, double, uint32_t, size_t)
+    """Argument count and kind (pointer, int, int64_t, double, uint32_t, size_t / uint64_t)
     of every binding in ``_lib.SIGNATURES`` against its prototype in vsr.h."""
     from vsr_gb300 import _lib
 

@@ -51,9 +51,9 @@ namespace vsr {
 
 size_t conv_tc_workspace(int kh, int kw);
 int conv_tc_supported(int kh, int kw);
-int run_conv_tc(const void* src, int dtype, int64_t H, int64_t W, int64_t pitch, const double* weights_host,
-                int kh, int kw, double nodata, int nodata_kind, void* dst, int out_dtype, int64_t out_pitch,
-                void* workspace, size_t ws_bytes, cudaStream_t st);
+int run_conv_tc(const void* src, int dtype, int bands, int64_t band_stride, int64_t H, int64_t W, int64_t pitch,
+                const double* weights_host, int kh, int kw, double nodata, int nodata_kind, void* dst, int out_dtype,
+                int64_t out_band_stride, int64_t out_pitch, void* workspace, size_t ws_bytes, cudaStream_t st);
 
 namespace {
 
@@ -184,6 +184,8 @@ struct TcArgs {
   const double* w64;            // the kernel as given (windows holding +-inf)
   int kh, kw;
   int nbuf, nst;
+  int bands;                    // band-first stack: tiles are band-major
+  int64_t band_stride, out_band_stride;
 };
 
 __device__ __forceinline__ int64_t clamp64(int64_t v, int64_t lo, int64_t hi) {
@@ -225,7 +227,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
       b_empty[kMaxStages], drain_bar;
   __shared__ uint32_t tmem_slot;
   __shared__ volatile int abort_flag;
-  __shared__ int64_t info_x0[2], info_y0[2];
+  __shared__ int64_t info_x0[2], info_y0[2], info_band[2];
   __shared__ float info_mu[2];
   __shared__ int info_nan[2], info_inf[2], info_nd[2];
   unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tc_raw) + 1023) & ~uintptr_t(1023));
@@ -233,7 +235,8 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
   const TcPlan L = make_plan(g, ND != 0, a.nbuf, a.nst);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t tiles_x = (a.W + kTN - 1) / kTN;
-  const int64_t total = tiles_x * ((a.H + kM - 1) / kM);
+  const int64_t per_band = tiles_x * ((a.H + kM - 1) / kM);
+  const int64_t total = per_band * a.bands;
   const uint32_t s_base = smem_u32(sm);
   double* sat = reinterpret_cast<double*>(sm + L.sat);
 
@@ -405,7 +408,8 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
         return;
       }
       tc_fence_after();
-      const int64_t x0 = info_x0[slot], y0 = info_y0[slot];
+      const int64_t x0 = info_x0[slot], y0 = info_y0[slot], band = info_band[slot];
+      const float* bsrc = a.src + band * a.band_stride;
       const float mu = info_mu[slot];
       const bool den_mma = info_nd[slot] != 0;
       const int64_t y = y0 + m;
@@ -483,14 +487,14 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
           for (uint32_t r = ib & ~ndm; r; r &= r - 1) {  // windows holding +-inf (rare)
             const int n = __ffs(r) - 1;
             if (xb + n < a.W) {
-              const float v = inf_window(a.src, a.H, a.W, a.pitch, a.w64, a.kh, a.kw, a.nd_kind, a.nd_f, y, xb + n);
+              const float v = inf_window(bsrc, a.H, a.W, a.pitch, a.w64, a.kh, a.kw, a.nd_kind, a.nd_f, y, xb + n);
 #pragma unroll
               for (int q = 0; q < 16; ++q)
                 if (q == n) num[q] = v;
             }
           }
           if (a.out_dtype == VSR_F64) {
-            double* row = static_cast<double*>(a.dst) + y * a.out_pitch + xb;
+            double* row = static_cast<double*>(a.dst) + band * a.out_band_stride + y * a.out_pitch + xb;
 #pragma unroll
             for (int n = 0; n < 16; ++n)
               if (xb + n < a.W) row[n] = ((ndm >> n) & 1u) ? a.nd_out : static_cast<double>(num[n]);
@@ -498,7 +502,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
             const float ndf = static_cast<float>(a.nd_out);
 #pragma unroll
             for (int n = 0; n < 16; ++n) num[n] = ((ndm >> n) & 1u) ? ndf : num[n];
-            float* row = static_cast<float*>(a.dst) + y * a.out_pitch + xb;
+            float* row = static_cast<float*>(a.dst) + band * a.out_band_stride + y * a.out_pitch + xb;
             if (a.vec_out && xb + 16 <= a.W) {
 #pragma unroll
               for (int q = 0; q < 4; ++q)
@@ -525,15 +529,17 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
           break;
         }
       }
-      const int64_t ty = t / tiles_x;
-      const int64_t x0 = (t - ty * tiles_x) * kTN, y0 = ty * kM;
+      const int64_t band = t / per_band, rem = t - band * per_band;
+      const int64_t ty = rem / tiles_x;
+      const int64_t x0 = (rem - ty * tiles_x) * kTN, y0 = ty * kM;
+      const float* bsrc = a.src + band * a.band_stride;
       const int64_t gx0 = x0 - kw2, gy0 = y0 - kh2;
       float mu = 0.0f;
       {
         // the window's centre pixel, moved inside the raster on edge tiles
         // (a centre far from the tile's values would cost accumulator bits)
         const int64_t yy = clamp64(gy0 + g.R / 2, 0, a.H - 1), xx = clamp64(gx0 + g.KW / 2, 0, a.W - 1);
-        const float v = __ldg(a.src + yy * a.pitch + xx);
+        const float v = __ldg(bsrc + yy * a.pitch + xx);
         const bool nd = ND == 1 ? v == a.nd_f : (ND == 2 ? v != v : false);
         if (!nd && isfinite(v)) mu = v;
       }
@@ -561,7 +567,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
           const uint32_t in = (rho < g.R && yy >= 0 && yy < a.H) ? colv : 0u;
           const int64_t base = (in ? yy : 0) * a.pitch + gx0 + kp0;
 #pragma unroll
-          for (int q = 0; q < 4; ++q) vb[r][q] = ((in >> q) & 1u) ? __ldg(a.src + base + q) : 0.0f;
+          for (int q = 0; q < 4; ++q) vb[r][q] = ((in >> q) & 1u) ? __ldg(bsrc + base + q) : 0.0f;
         }
 #pragma unroll
         for (int r = 0; r < kConvRows; ++r) {
@@ -637,6 +643,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
       if (ct == 0) {
         info_x0[slot] = x0;
         info_y0[slot] = y0;
+        info_band[slot] = band;
         info_mu[slot] = mu;
         info_nan[slot] = tile_nan;
         info_inf[slot] = tile_inf;
@@ -762,9 +769,9 @@ size_t conv_tc_workspace(int kh, int kw) {
   return a + b + c;
 }
 
-int run_conv_tc(const void* src, int dtype, int64_t H, int64_t W, int64_t pitch, const double* weights_host, int kh,
-                int kw, double nodata, int nodata_kind, void* dst, int out_dtype, int64_t out_pitch, void* workspace,
-                size_t ws_bytes, cudaStream_t st) {
+int run_conv_tc(const void* src, int dtype, int bands, int64_t band_stride, int64_t H, int64_t W, int64_t pitch,
+                const double* weights_host, int kh, int kw, double nodata, int nodata_kind, void* dst, int out_dtype,
+                int64_t out_band_stride, int64_t out_pitch, void* workspace, size_t ws_bytes, cudaStream_t st) {
   if (dtype != VSR_F32) return fail(VSR_ERR_UNSUPPORTED, "split-BF16 convolution reads float32 rasters");
   if (!conv_tc_supported(kh, kw))
     return fail(VSR_ERR_UNSUPPORTED, "split-BF16 convolution supports kernels up to %dx%d", kMaxTCK, kMaxTCK);
@@ -792,14 +799,16 @@ int run_conv_tc(const void* src, int dtype, int64_t H, int64_t W, int64_t pitch,
   VSR_CUDA_TRY(cudaGetLastError());
   uint32_t* err = device_error_word();
   if (!err) return VSR_ERR_CUDA;
-  const bool vec_out = out_dtype == VSR_F32 && aligned(dst, 16) && out_pitch % 4 == 0;
+  const bool vec_out =
+      out_dtype == VSR_F32 && aligned(dst, 16) && out_pitch % 4 == 0 && (bands == 1 || out_band_stride % 4 == 0);
   TcArgs a{static_cast<const float*>(src), H, W, pitch, kind, static_cast<float>(ndv), nodata, dst, out_dtype,
-           out_pitch, vec_out ? 1 : 0, reinterpret_cast<const unsigned char*>(img), sat, w64, kh, kw, nbuf, nst};
+           out_pitch, vec_out ? 1 : 0, reinterpret_cast<const unsigned char*>(img), sat, w64, kh, kw, nbuf, nst,
+           bands, bands > 1 ? band_stride : 0, bands > 1 ? out_band_stride : 0};
   // At least 116 KB of shared memory keeps one CTA (and its 512 TMEM columns) per SM.
   const size_t smem = std::max<size_t>(L.total + 1024, 116 * 1024);
   auto kern = kind == VSR_NODATA_NONE ? conv_tc_kernel<0> : (kind == VSR_NODATA_VALUE ? conv_tc_kernel<1> : conv_tc_kernel<2>);
   VSR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-  const int64_t tiles = ((W + kTN - 1) / kTN) * ((H + kM - 1) / kM);
+  const int64_t tiles = ((W + kTN - 1) / kTN) * ((H + kM - 1) / kM) * bands;
   const int64_t grid = std::min<int64_t>(tiles, sm_count());
   kern<<<static_cast<unsigned>(grid), kThreadsTC, smem, st>>>(a, err);
   VSR_CUDA_TRY(cudaGetLastError());

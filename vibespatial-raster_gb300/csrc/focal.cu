@@ -1252,9 +1252,9 @@ using namespace vsr;
 namespace vsr {
 size_t conv_tc_workspace(int kh, int kw);  // conv_tc.cu
 int conv_tc_supported(int kh, int kw);
-int run_conv_tc(const void* src, int dtype, int64_t H, int64_t W, int64_t pitch, const double* weights_host,
-                int kh, int kw, double nodata, int nodata_kind, void* dst, int out_dtype, int64_t out_pitch,
-                void* workspace, size_t ws_bytes, cudaStream_t st);
+int run_conv_tc(const void* src, int dtype, int bands, int64_t band_stride, int64_t H, int64_t W, int64_t pitch,
+                const double* weights_host, int kh, int kw, double nodata, int nodata_kind, void* dst, int out_dtype,
+                int64_t out_band_stride, int64_t out_pitch, void* workspace, size_t ws_bytes, cudaStream_t st);
 int gauss_tc_supported(int dtype, int k);  // gauss_tc.cu
 size_t gauss_tc_workspace(int64_t H, int64_t W, int dtype, int k);
 int run_gauss_tc(const void* src, int dtype, int bands, int64_t band_stride, int64_t H, int64_t W, int64_t pitch,
@@ -1269,12 +1269,16 @@ extern "C" size_t vsr_convolve_workspace_size(int kh, int kw, int precision) {
   return n;
 }
 
-extern "C" int vsr_convolve(const void* src, int dtype, int64_t height, int64_t width, int64_t pitch,
-                            const double* weights_host, int kh, int kw, double nodata, int nodata_kind,
-                            void* dst, int out_dtype, int64_t out_pitch, int precision, void* workspace,
-                            size_t workspace_bytes, void* stream) {
+extern "C" int vsr_convolve_bands(const void* src, int dtype, int bands, int64_t band_stride, int64_t height,
+                                  int64_t width, int64_t pitch, const double* weights_host, int kh, int kw,
+                                  double nodata, int nodata_kind, void* dst, int out_dtype, int64_t out_band_stride,
+                                  int64_t out_pitch, int precision, void* workspace, size_t workspace_bytes,
+                                  void* stream) {
+  if (bands < 1 || bands > 65535) return fail(VSR_ERR_INVALID_ARG, "bands must be in [1, 65535]");
   int rc = check_raster(src, dtype, height, width, pitch, dst, out_dtype, out_pitch);
   if (rc || height == 0 || width == 0) return rc;
+  if (bands > 1 && (band_stride < pitch * height || out_band_stride < out_pitch * height))
+    return fail(VSR_ERR_INVALID_ARG, "band strides smaller than one band");
   if (!weights_host) return fail(VSR_ERR_INVALID_ARG, "weights_host is NULL");
   if (kh <= 0 || kw <= 0) return fail(VSR_ERR_INVALID_ARG, "kernel must be at least 1 x 1");
   if (precision < VSR_PREC_AUTO || precision > VSR_PREC_SPLIT_BF16) return fail(VSR_ERR_INVALID_ARG, "bad precision %d", precision);
@@ -1297,8 +1301,9 @@ extern "C" int vsr_convolve(const void* src, int dtype, int64_t height, int64_t 
     well_conditioned = sa <= 4.0 * std::fabs(s);
   }
   if (precision == VSR_PREC_SPLIT_BF16 || well_conditioned)
-    return run_conv_tc(src, dtype, height, width, pitch, weights_host, kh, kw, nodata, nodata_kind, dst, out_dtype,
-                       out_pitch, workspace, workspace_bytes, static_cast<cudaStream_t>(stream));
+    return run_conv_tc(src, dtype, bands, band_stride, height, width, pitch, weights_host, kh, kw, nodata,
+                       nodata_kind, dst, out_dtype, out_band_stride, out_pitch, workspace, workspace_bytes,
+                       static_cast<cudaStream_t>(stream));
   const size_t need = conv_ws_plain(kh, kw);
   if (!workspace || workspace_bytes < need || !aligned(workspace, 256))
     return fail(VSR_ERR_WORKSPACE, "workspace must be 256-byte aligned and >= %zu bytes", need);
@@ -1312,8 +1317,16 @@ extern "C" int vsr_convolve(const void* src, int dtype, int64_t height, int64_t 
   prep_weights<<<1, 256, 0, st>>>(w64, kh, kw, kw4, w32, wsum);
   VSR_CUDA_TRY(cudaGetLastError());
   ConvArgs a{src, dtype, height, width, pitch, make_nodata(dtype, nodata, nodata_kind), w32, wsum, kh, kw, kw4,
-             nodata, dst, out_dtype, out_pitch};
-  return run_conv_direct(a, st);
+             nodata, dst, out_dtype, out_pitch, bands > 1 ? band_stride : 0, bands > 1 ? out_band_stride : 0};
+  return run_conv_direct(a, st, bands);
+}
+
+extern "C" int vsr_convolve(const void* src, int dtype, int64_t height, int64_t width, int64_t pitch,
+                            const double* weights_host, int kh, int kw, double nodata, int nodata_kind,
+                            void* dst, int out_dtype, int64_t out_pitch, int precision, void* workspace,
+                            size_t workspace_bytes, void* stream) {
+  return vsr_convolve_bands(src, dtype, 1, 0, height, width, pitch, weights_host, kh, kw, nodata, nodata_kind, dst,
+                            out_dtype, 0, out_pitch, precision, workspace, workspace_bytes, stream);
 }
 
 // Gaussian workspace: g (k4 floats) | dense weights (k x k4 floats) | total.
@@ -1430,6 +1443,15 @@ static int focal_mean_impl(const void* src, int dtype, int bands, int64_t band_s
     default: return launch_box<AccD>(a, st, bands);
   }
 }
+
+namespace vsr {
+int focal_mean_bands_impl(const void* src, int dtype, int bands, int64_t band_stride, int64_t height, int64_t width,
+                          int64_t pitch, int radius_y, int radius_x, double nodata, int nodata_kind, void* dst,
+                          int out_dtype, int64_t out_band_stride, int64_t out_pitch, void* stream) {
+  return focal_mean_impl(src, dtype, bands, band_stride, height, width, pitch, radius_y, radius_x, nodata,
+                         nodata_kind, dst, out_dtype, out_band_stride, out_pitch, stream);
+}
+}  // namespace vsr
 
 extern "C" int vsr_focal_mean(const void* src, int dtype, int64_t height, int64_t width, int64_t pitch,
                               int radius_y, int radius_x, double nodata, int nodata_kind, void* dst, int out_dtype,

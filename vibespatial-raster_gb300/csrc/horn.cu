@@ -57,6 +57,11 @@ __global__ void __launch_bounds__(256) horn_generic(const T* __restrict__ src, c
   const int64_t x = static_cast<int64_t>(blockIdx.x) * 32 + threadIdx.x;
   const int64_t y = static_cast<int64_t>(blockIdx.y) * 8 + threadIdx.y;
   if (x >= P.width || y >= P.height) return;
+  const int64_t band = blockIdx.z;
+  src += band * P.in_band_stride;
+  if (slope) slope += band * P.out_band_stride;
+  if (aspect) aspect += band * P.out_band_stride;
+  if (hs) hs += band * P.hs_band_stride;
   const MaskRule rule = mask_rule(P);
   D v[3][3];
   bool dil = false, ctr = false;
@@ -93,7 +98,8 @@ int launch_generic(const void* src, const HornParams& P, double ndv, void* slope
                    uint8_t* hs, cudaStream_t st) {
   NodataTest<T> nd{P.nd_kind, static_cast<T>(ndv)};
   dim3 block(32, 8);
-  dim3 grid(static_cast<unsigned>((P.width + 31) / 32), static_cast<unsigned>((P.height + 7) / 8));
+  dim3 grid(static_cast<unsigned>((P.width + 31) / 32), static_cast<unsigned>((P.height + 7) / 8),
+            static_cast<unsigned>(P.bands));
   if (grid.y > 65535u) return fail(VSR_ERR_UNSUPPORTED, "raster height %lld too large for the generic Horn path", (long long)P.height);
   horn_generic<T, O><<<grid, block, 0, st>>>(static_cast<const T*>(src), P, nd, static_cast<O*>(slope),
                                              static_cast<O*>(aspect), hs);
@@ -133,8 +139,10 @@ int launch_tma_config(int cfg, const void* src, const HornParams& P, float nd_in
   const int want = (slope ? kWantSlope : 0) | (aspect ? kWantAspect : 0) | (hs ? kWantHs : 0);
   // the partial output sets run the 64-row shape (horn_tma.cuh)
   const int box_h = (want == 7 ? th : 64) + 2;
-  int rc = encode_tensor_map_2d(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, src, P.width, P.height, P.in_pitch, kSW,
-                                static_cast<uint32_t>(box_h));
+  const uint64_t plane = P.bands > 1 ? static_cast<uint64_t>(P.in_band_stride)
+                                     : static_cast<uint64_t>(P.in_pitch) * static_cast<uint64_t>(P.height);
+  int rc = encode_tensor_map_3d(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, src, P.width, P.height, P.bands, P.in_pitch,
+                                plane, kSW, static_cast<uint32_t>(box_h));
   if (rc) return rc;
   uint32_t* err = device_error_word();
   if (!err) return VSR_ERR_CUDA;
@@ -156,14 +164,16 @@ int horn_config_count() { return horn::kNumHornConfigs; }
 
 }  // namespace vsr
 
-extern "C" int vsr_horn_fused(const void* dem, int dtype, int64_t height, int64_t width, int64_t pitch,
-                              double cell_x, double cell_y, double nodata, int nodata_kind,
-                              uint32_t flags, void* slope, void* aspect, int out_dtype,
-                              int64_t out_pitch, uint8_t* hillshade, int64_t hs_pitch,
-                              double z_factor, double zenith_rad, double azimuth_rad, void* stream) {
+extern "C" int vsr_horn_fused_bands(const void* dem, int dtype, int bands, int64_t band_stride, int64_t height,
+                                    int64_t width, int64_t pitch, double cell_x, double cell_y, double nodata,
+                                    int nodata_kind, uint32_t flags, void* slope, void* aspect, int out_dtype,
+                                    int64_t out_band_stride, int64_t out_pitch, uint8_t* hillshade,
+                                    int64_t hs_band_stride, int64_t hs_pitch, double z_factor, double zenith_rad,
+                                    double azimuth_rad, void* stream) {
   using namespace vsr;
   using namespace vsr::horn;
   if (height < 0 || width < 0) return fail(VSR_ERR_INVALID_ARG, "negative raster size");
+  if (bands < 1 || bands > 65535) return fail(VSR_ERR_INVALID_ARG, "bands must be in [1, 65535]");
   if (height == 0 || width == 0) return VSR_OK;
   if (!slope && !aspect && !hillshade) return VSR_OK;
   if (!dem) return fail(VSR_ERR_INVALID_ARG, "dem is NULL");
@@ -173,6 +183,9 @@ extern "C" int vsr_horn_fused(const void* dem, int dtype, int64_t height, int64_
     return fail(VSR_ERR_INVALID_ARG, "slope/aspect out_dtype must be VSR_F32 or VSR_F64");
   if ((slope || aspect) && out_pitch < width) return fail(VSR_ERR_INVALID_ARG, "out_pitch < width");
   if (hillshade && hs_pitch < width) return fail(VSR_ERR_INVALID_ARG, "hs_pitch < width");
+  if (bands > 1 && (band_stride < pitch * height || ((slope || aspect) && out_band_stride < out_pitch * height) ||
+                    (hillshade && hs_band_stride < hs_pitch * height)))
+    return fail(VSR_ERR_INVALID_ARG, "band strides smaller than one band");
   if (!(cell_x > 0.0) || !(cell_y > 0.0) || !std::isfinite(cell_x) || !std::isfinite(cell_y))
     return fail(VSR_ERR_INVALID_ARG, "cell sizes must be positive and finite");
   if (nodata_kind < VSR_NODATA_NONE || nodata_kind > VSR_NODATA_NAN)
@@ -189,6 +202,10 @@ extern "C" int vsr_horn_fused(const void* dem, int dtype, int64_t height, int64_
   P.in_pitch = pitch;
   P.out_pitch = out_pitch;
   P.hs_pitch = hs_pitch;
+  P.bands = bands;
+  P.in_band_stride = bands > 1 ? band_stride : 0;
+  P.out_band_stride = bands > 1 ? out_band_stride : 0;
+  P.hs_band_stride = bands > 1 ? hs_band_stride : 0;
   P.inv8cx = static_cast<float>(1.0 / (8.0 * cell_x));
   P.inv8cy = static_cast<float>(1.0 / (8.0 * cell_y));
   P.zf = static_cast<float>(z_factor);
@@ -207,6 +224,8 @@ extern "C" int vsr_horn_fused(const void* dem, int dtype, int64_t height, int64_
                       aligned(dem, 16) && pitch % 4 == 0 && (!slope || aligned(slope, 16)) &&
                       (!aspect || aligned(aspect, 16)) && (!(slope || aspect) || out_pitch % 4 == 0) &&
                       (!hillshade || (aligned(hillshade, 4) && hs_pitch % 4 == 0)) &&
+                      (bands == 1 || (band_stride % 4 == 0 && (!(slope || aspect) || out_band_stride % 4 == 0) &&
+                                      (!hillshade || hs_band_stride % 4 == 0))) &&
                       width < (int64_t(1) << 31) && height < (int64_t(1) << 31);
   if (tma_ok)
     return launch_tma_config(tuning_get(VSR_OP_HORN), dem, P, static_cast<float>(ndv),
@@ -216,3 +235,12 @@ extern "C" int vsr_horn_fused(const void* dem, int dtype, int64_t height, int64_
   return dispatch_generic<float>(dtype, dem, P, ndv, slope, aspect, hillshade, st);
 }
 
+
+extern "C" int vsr_horn_fused(const void* dem, int dtype, int64_t height, int64_t width, int64_t pitch,
+                              double cell_x, double cell_y, double nodata, int nodata_kind, uint32_t flags,
+                              void* slope, void* aspect, int out_dtype, int64_t out_pitch, uint8_t* hillshade,
+                              int64_t hs_pitch, double z_factor, double zenith_rad, double azimuth_rad, void* stream) {
+  return vsr_horn_fused_bands(dem, dtype, 1, 0, height, width, pitch, cell_x, cell_y, nodata, nodata_kind, flags,
+                              slope, aspect, out_dtype, 0, out_pitch, hillshade, 0, hs_pitch, z_factor, zenith_rad,
+                              azimuth_rad, stream);
+}

@@ -33,6 +33,8 @@ namespace horn {
 struct HornParams {
   int64_t height, width;
   int64_t in_pitch, out_pitch, hs_pitch;
+  int bands;  // band-first stack: band b at b * *_band_stride elements
+  int64_t in_band_stride, out_band_stride, hs_band_stride;
   float inv8cx, inv8cy;  // 1 / (8 cell) from FP64
   float zf, zf2;
   float cos_z, hs_a, hs_b;  // cos(zen); sin(zen) cos(az) zf; sin(zen) sin(az) zf

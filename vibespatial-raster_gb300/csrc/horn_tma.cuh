@@ -4,10 +4,10 @@
 // (horn_tma_all.cu: slope + aspect + hillshade; horn_tma_sub.cu: the others),
 // so the instantiations compile in parallel.
 //
-// Persistent CTAs walk 128 x TH output tiles; each tile plus a 4-column /
-// 1-row halo is staged into shared memory by a 2-D TMA load (multi-stage
-// mbarrier pipeline), edge replication is patched in shared memory on border
-// tiles, each lane computes 4 adjacent pixels per row from a rolling 3-row
+// Persistent CTAs walk the 128 x TH output tiles of every band (band-major);
+// each tile plus a 4-column / 1-row halo is staged into shared memory by a
+// 3-D TMA load (x, y, band; multi-stage mbarrier pipeline), edge replication
+// is patched in shared memory on border tiles, each lane computes 4 adjacent pixels per row from a rolling 3-row
 // register window (horn_rows) and writes 128-bit slope/aspect and 32-bit
 // hillshade streaming stores.
 #pragma once
@@ -41,14 +41,16 @@ __global__ void __launch_bounds__(THREADS, MINB) horn_f32_tma(const __grid_const
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t W = P.width, H = P.height;
   const int64_t tiles_x = (W + kTW - 1) / kTW;
-  const int64_t total = tiles_x * ((H + TH - 1) / TH);
+  const int64_t per_band = tiles_x * ((H + TH - 1) / TH);
+  const int64_t total = per_band * P.bands;
   const MaskRule rule = mask_rule(P);
 
   auto issue = [&](int64_t t, int s) {
-    const int64_t ty = t / tiles_x, tx = t - ty * tiles_x;
+    const int64_t b = t / per_band, r = t - b * per_band;
+    const int64_t ty = r / tiles_x, tx = r - ty * tiles_x;
     mbar_arrive_expect_tx(&bars[s], Tile::kBytes);
-    tma_load_2d(reinterpret_cast<unsigned char*>(stages) + s * Tile::kStride, &tmap,
-                static_cast<int>(tx * kTW - 4), static_cast<int>(ty * TH - 1), &bars[s]);
+    tma_load_3d(reinterpret_cast<unsigned char*>(stages) + s * Tile::kStride, &tmap, static_cast<int>(tx * kTW - 4),
+                static_cast<int>(ty * TH - 1), static_cast<int>(b), &bars[s]);
   };
 
   if (tid == 0) {
@@ -84,7 +86,8 @@ __global__ void __launch_bounds__(THREADS, MINB) horn_f32_tma(const __grid_const
       return;
     }
     float* S = stages + s * (Tile::kStride / 4);
-    const int64_t ty = t / tiles_x, tx = t - ty * tiles_x;
+    const int64_t b = t / per_band, rem = t - b * per_band;
+    const int64_t ty = rem / tiles_x, tx = rem - ty * tiles_x;
     const int64_t x0 = tx * kTW, y0 = ty * TH;
 
     // Edge replication in shared memory (TMA fills out-of-range with zeros).
@@ -109,7 +112,9 @@ __global__ void __launch_bounds__(THREADS, MINB) horn_f32_tma(const __grid_const
     const int64_t xs = x0 + 4 * lane;
     const int r0 = warp * RB;
     const bool edge = x0 + kTW > W || y0 + TH > H;
-    const RowPtrs g = global_rows(slope, aspect, hs, P, y0 + r0, xs);
+    const RowPtrs g = global_rows(slope ? slope + b * P.out_band_stride : nullptr,
+                                  aspect ? aspect + b * P.out_band_stride : nullptr,
+                                  hs ? hs + b * P.hs_band_stride : nullptr, P, y0 + r0, xs);
     if (edge) horn_rows<RB, WANT, NDK, true, true>(S, lane, r0, y0, xs, P, rule, nd_in, g.s, g.a, g.h, P.out_pitch, P.hs_pitch);
     else horn_rows<RB, WANT, NDK, false, true>(S, lane, r0, y0, xs, P, rule, nd_in, g.s, g.a, g.h, P.out_pitch, P.hs_pitch);
 
@@ -134,7 +139,7 @@ int launch_tma_t(const CUtensorMap& map, const HornParams& P, float nd_in, float
   int per_sm = 0;
   VSR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, THREADS, smem));
   if (per_sm < 1) return fail(VSR_ERR_CUDA, "horn_f32_tma cannot be resident (smem %zu)", smem);
-  const int64_t tiles = ((P.width + kTW - 1) / kTW) * ((P.height + TH - 1) / TH);
+  const int64_t tiles = ((P.width + kTW - 1) / kTW) * ((P.height + TH - 1) / TH) * P.bands;
   const int64_t grid = std::min<int64_t>(tiles, static_cast<int64_t>(sm_count()) * per_sm);
   kern<<<static_cast<unsigned>(grid), THREADS, smem, st>>>(map, P, nd_in, slope, aspect, hs, err);
   VSR_CUDA_TRY(cudaGetLastError());

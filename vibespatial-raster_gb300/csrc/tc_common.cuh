@@ -94,12 +94,12 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 
 // Bounded wait that also gives up once another role has raised ``abort``.
 __device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, volatile int* abort, uint32_t* err,
-                                              uint32_t code) {
+                                              uint32_t code, uint64_t limit_ns = kWaitLimitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = global_timer_ns();
   while (!mbar_try_wait(bar, parity)) {
     if (*abort) return false;
-    if (global_timer_ns() - t0 > kWaitLimitNs) {
+    if (global_timer_ns() - t0 > limit_ns) {
       atomicOr(err, code);
       *abort = 1;
       return false;

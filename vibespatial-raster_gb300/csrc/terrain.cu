@@ -35,6 +35,7 @@ constexpr int kDSW = kDTW + 2, kDSH = kDTH + 2;
 
 struct DerivParams {
   int64_t H, W, pitch, out_pitch;
+  int64_t band_stride, out_band_stride;  // band blockIdx.z of a band-first stack
   int nd_kind;      // resolved VSR_NODATA_*
   double nd_in;     // nodata value of the raster (element value, as double)
   double nd_out;    // value written to nodata / border pixels
@@ -119,6 +120,7 @@ __global__ void __launch_bounds__(kDTW * kDTH) terrain_deriv_kernel(const T* __r
   __shared__ C tile[kDSH][kDSW + 1];
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kDTW + tx;
   const int64_t x0 = static_cast<int64_t>(blockIdx.x) * kDTW, y0 = static_cast<int64_t>(blockIdx.y) * kDTH;
+  src += static_cast<int64_t>(blockIdx.z) * P.band_stride;
   // the tile and its 1-pixel halo, coordinates clamped (edge replication)
   for (int i = tid; i < kDSH * kDSW; i += kDTW * kDTH) {
     const int r = i / kDSW, c = i - r * kDSW;
@@ -130,7 +132,7 @@ __global__ void __launch_bounds__(kDTW * kDTH) terrain_deriv_kernel(const T* __r
   __syncthreads();
   const int64_t x = x0 + tx, y = y0 + ty;
   if (x >= P.W || y >= P.H) return;
-  const int64_t o = y * P.out_pitch + x;
+  const int64_t o = static_cast<int64_t>(blockIdx.z) * P.out_band_stride + y * P.out_pitch + x;
   C z[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) z[k] = tile[ty + k / 3][tx + k % 3];
@@ -202,8 +204,9 @@ __global__ void __launch_bounds__(kDTW * kDTH) terrain_deriv_kernel(const T* __r
 }
 
 template <typename T>
-int launch_deriv(const void* src, const DerivParams& P, cudaStream_t st) {
-  const dim3 grid(static_cast<unsigned>((P.W + kDTW - 1) / kDTW), static_cast<unsigned>((P.H + kDTH - 1) / kDTH));
+int launch_deriv(const void* src, const DerivParams& P, int bands, cudaStream_t st) {
+  const dim3 grid(static_cast<unsigned>((P.W + kDTW - 1) / kDTW), static_cast<unsigned>((P.H + kDTH - 1) / kDTH),
+                  static_cast<unsigned>(bands));
   if (grid.y > 65535u) return fail(VSR_ERR_UNSUPPORTED, "raster too tall for the terrain-derivative grid");
   terrain_deriv_kernel<T><<<grid, dim3(kDTW, kDTH), 0, st>>>(static_cast<const T*>(src), P);
   VSR_CUDA_TRY(cudaGetLastError());
@@ -215,11 +218,13 @@ int launch_deriv(const void* src, const DerivParams& P, cudaStream_t st) {
 
 using namespace vsr;
 
-extern "C" int vsr_terrain_derivatives(const void* dem, int dtype, int64_t height, int64_t width, int64_t pitch,
-                                       double cell_x, double cell_y, double nodata, int nodata_kind,
-                                       double nodata_out, void* tri, void* tpi, void* curvature, int out_dtype,
-                                       int64_t out_pitch, void* stream) {
+extern "C" int vsr_terrain_derivatives_bands(const void* dem, int dtype, int bands, int64_t band_stride,
+                                             int64_t height, int64_t width, int64_t pitch, double cell_x,
+                                             double cell_y, double nodata, int nodata_kind, double nodata_out,
+                                             void* tri, void* tpi, void* curvature, int out_dtype,
+                                             int64_t out_band_stride, int64_t out_pitch, void* stream) {
   if (height < 0 || width < 0) return fail(VSR_ERR_INVALID_ARG, "negative raster size");
+  if (bands < 1 || bands > 65535) return fail(VSR_ERR_INVALID_ARG, "bands must be in [1, 65535]");
   if (height == 0 || width == 0 || (!tri && !tpi && !curvature)) return VSR_OK;
   if (!dem) return fail(VSR_ERR_INVALID_ARG, "dem is NULL");
   const size_t es = dtype_size(dtype);
@@ -227,6 +232,8 @@ extern "C" int vsr_terrain_derivatives(const void* dem, int dtype, int64_t heigh
   if (pitch < width) return fail(VSR_ERR_INVALID_ARG, "pitch %lld < width %lld", (long long)pitch, (long long)width);
   if (out_dtype != VSR_F32 && out_dtype != VSR_F64) return fail(VSR_ERR_INVALID_ARG, "out_dtype must be VSR_F32 or VSR_F64");
   if (out_pitch < width) return fail(VSR_ERR_INVALID_ARG, "out_pitch < width");
+  if (bands > 1 && (band_stride < pitch * height || out_band_stride < out_pitch * height))
+    return fail(VSR_ERR_INVALID_ARG, "band strides smaller than one band");
   if (!(cell_x > 0.0) || !(cell_y > 0.0) || !std::isfinite(cell_x) || !std::isfinite(cell_y))
     return fail(VSR_ERR_INVALID_ARG, "cell sizes must be positive and finite");
   if (nodata_kind < VSR_NODATA_NONE || nodata_kind > VSR_NODATA_NAN)
@@ -240,6 +247,8 @@ extern "C" int vsr_terrain_derivatives(const void* dem, int dtype, int64_t heigh
   P.W = width;
   P.pitch = pitch;
   P.out_pitch = out_pitch;
+  P.band_stride = bands > 1 ? band_stride : 0;
+  P.out_band_stride = bands > 1 ? out_band_stride : 0;
   P.nd_kind = resolve_nodata(dtype, nodata, nodata_kind, &P.nd_in);
   P.nd_out = nodata_out;
   P.cx2 = cell_x * cell_x;
@@ -255,11 +264,19 @@ extern "C" int vsr_terrain_derivatives(const void* dem, int dtype, int64_t heigh
   P.out_dtype = out_dtype;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   switch (dtype) {
-    case VSR_U8: return launch_deriv<uint8_t>(dem, P, st);
-    case VSR_I16: return launch_deriv<int16_t>(dem, P, st);
-    case VSR_U16: return launch_deriv<uint16_t>(dem, P, st);
-    case VSR_I32: return launch_deriv<int32_t>(dem, P, st);
-    case VSR_F32: return launch_deriv<float>(dem, P, st);
-    default: return launch_deriv<double>(dem, P, st);
+    case VSR_U8: return launch_deriv<uint8_t>(dem, P, bands, st);
+    case VSR_I16: return launch_deriv<int16_t>(dem, P, bands, st);
+    case VSR_U16: return launch_deriv<uint16_t>(dem, P, bands, st);
+    case VSR_I32: return launch_deriv<int32_t>(dem, P, bands, st);
+    case VSR_F32: return launch_deriv<float>(dem, P, bands, st);
+    default: return launch_deriv<double>(dem, P, bands, st);
   }
+}
+
+extern "C" int vsr_terrain_derivatives(const void* dem, int dtype, int64_t height, int64_t width, int64_t pitch,
+                                       double cell_x, double cell_y, double nodata, int nodata_kind,
+                                       double nodata_out, void* tri, void* tpi, void* curvature, int out_dtype,
+                                       int64_t out_pitch, void* stream) {
+  return vsr_terrain_derivatives_bands(dem, dtype, 1, 0, height, width, pitch, cell_x, cell_y, nodata, nodata_kind,
+                                       nodata_out, tri, tpi, curvature, out_dtype, 0, out_pitch, stream);
 }

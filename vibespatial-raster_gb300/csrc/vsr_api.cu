@@ -140,6 +140,22 @@ int encode_tensor_map_2d(CUtensorMap* map, CUtensorMapDataType type, size_t elem
   return VSR_OK;
 }
 
+int encode_tensor_map_3d(CUtensorMap* map, CUtensorMapDataType type, size_t elem_bytes, const void* base,
+                         uint64_t width, uint64_t height, uint64_t depth, uint64_t pitch_elems, uint64_t plane_elems,
+                         uint32_t box_w, uint32_t box_h) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return fail(VSR_ERR_CUDA, "cuTensorMapEncodeTiled entry point unavailable");
+  cuuint64_t dims[3] = {width, height, depth};
+  cuuint64_t strides[2] = {pitch_elems * elem_bytes, plane_elems * elem_bytes};
+  cuuint32_t box[3] = {box_w, box_h, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = fn(map, type, 3, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    return fail(VSR_ERR_CUDA, "cuTensorMapEncodeTiled (3-D) failed (CUresult %d)", static_cast<int>(r));
+  return VSR_OK;
+}
+
 // Selected launch configuration per tunable operation (process-wide).
 static std::atomic<int> g_tuning[VSR_OP_COUNT];
 

@@ -31,10 +31,10 @@ int cuda_fail(cudaError_t e, const char* what);
 // file-scope __device__ variable of vsr_api.cu; kernels receive its device
 // address (device_error_word(), resolved once per device) as a parameter.
 enum DeviceError : uint32_t {
-  kDevErrTmaTimeout = 1u,
-  kDevErrMmaTimeout = 2u,
-  kDevErrQueue = 4u,
-  kDevErrPlan = 8u,  // a batch launch whose shape differs from its plan's
+  kDevErrTmaTimeout = VSR_DEVERR_TMA_TIMEOUT,
+  kDevErrMmaTimeout = VSR_DEVERR_MMA_TIMEOUT,
+  kDevErrQueue = VSR_DEVERR_QUEUE,
+  kDevErrPlan = VSR_DEVERR_PLAN,  // a batch launch whose shape differs from its plan's
 };
 uint32_t* device_error_word();  // nullptr (and error set) on failure
 
@@ -112,13 +112,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 
 // Bounded wait on an mbarrier phase.  Returns false (and ORs ``code`` into
-// *err_word) if the phase did not complete within kWaitLimitNs.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
-                                                  uint32_t* err_word, uint32_t code) {
+// *err_word) if the phase did not complete within ``limit_ns`` (default
+// kWaitLimitNs).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t* err_word,
+                                                  uint32_t code, uint64_t limit_ns = kWaitLimitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = global_timer_ns();
   while (!mbar_try_wait(bar, parity)) {
-    if (global_timer_ns() - t0 > kWaitLimitNs) {
+    if (global_timer_ns() - t0 > limit_ns) {
       atomicOr(err_word, code);
       return false;
     }
@@ -163,6 +164,15 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
+// 3-D tiled TMA load of box (x, y, z) into shared memory, completing on ``bar``.
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
 // 2-D tiled TMA store of box (x, y) from shared memory, tracked by the
 // thread's bulk async-groups (bulk_commit / bulk_wait_read).  x * element
 // size must be a multiple of 16 bytes; the box is clipped at the tensor edge.
@@ -202,6 +212,12 @@ __device__ __forceinline__ void prefetch_tensormap(const CUtensorMap* map) {
 // dependency on libcuda).
 int encode_tensor_map_2d(CUtensorMap* map, CUtensorMapDataType type, size_t elem_bytes,
                          const void* base, uint64_t width, uint64_t height, uint64_t pitch_elems,
+                         uint32_t box_w, uint32_t box_h);
+
+// 3-D map (x = width, y = height, z = depth planes ``plane_elems`` apart)
+// with a box_w x box_h x 1 box.
+int encode_tensor_map_3d(CUtensorMap* map, CUtensorMapDataType type, size_t elem_bytes, const void* base,
+                         uint64_t width, uint64_t height, uint64_t depth, uint64_t pitch_elems, uint64_t plane_elems,
                          uint32_t box_w, uint32_t box_h);
 
 inline bool aligned(const void* p, size_t a) {

@@ -13,7 +13,12 @@ from vsr_gb300.algebra import (  # noqa: F401
     raster_aspect,
     raster_convolve,
     raster_curvature,
+    raster_focal_max,
     raster_focal_mean,
+    raster_focal_min,
+    raster_focal_range,
+    raster_focal_std,
+    raster_focal_variety,
     raster_gaussian_filter,
     raster_hillshade,
     raster_slope,
@@ -45,7 +50,12 @@ __all__ = [
     "raster_aspect",
     "raster_convolve",
     "raster_curvature",
+    "raster_focal_max",
     "raster_focal_mean",
+    "raster_focal_min",
+    "raster_focal_range",
+    "raster_focal_std",
+    "raster_focal_variety",
     "raster_gaussian_filter",
     "raster_hillshade",
     "raster_slope",

@@ -27,6 +27,8 @@ VSR_HORN_CENTER_ONLY = 1
 VSR_HORN_SA_NAN_UNMASKED = 2
 VSR_PREC_AUTO, VSR_PREC_FP32, VSR_PREC_SPLIT_BF16 = 0, 1, 2
 VSR_OP_HORN, VSR_OP_BATCH = 1, 2
+VSR_DEVERR_TMA_TIMEOUT, VSR_DEVERR_MMA_TIMEOUT, VSR_DEVERR_QUEUE, VSR_DEVERR_PLAN = 1, 2, 4, 8
+VSR_STAT = {"min": 0, "max": 1, "mean": 2, "std": 3, "range": 4, "variety": 5}
 
 DTYPE_CODES = {
     np.dtype(np.uint8): VSR_U8,
@@ -51,6 +53,7 @@ SIGNATURES: dict[str, tuple] = {
     "vsr_last_error": (_c.c_char_p, []),
     "vsr_device_info": (_int, [_c.POINTER(_int), _c.POINTER(_int), _c.POINTER(_int)]),
     "vsr_poll_device_error": (_int, [_vp, _c.POINTER(_u32)]),
+    "vsr_wait_selftest": (_int, [_c.c_uint64, _vp, _vp]),
     "vsr_tuning_count": (_int, [_int]),
     "vsr_tuning_set": (_int, [_int, _int]),
     "vsr_tuning_get": (_int, [_int]),
@@ -58,6 +61,21 @@ SIGNATURES: dict[str, tuple] = {
         _int,
         [_vp, _int, _i64, _i64, _i64, _dbl, _dbl, _dbl, _int, _u32, _vp, _vp, _int, _i64, _vp, _i64,
          _dbl, _dbl, _dbl, _vp],
+    ),
+    "vsr_horn_fused_bands": (
+        _int,
+        [_vp, _int, _int, _i64, _i64, _i64, _i64, _dbl, _dbl, _dbl, _int, _u32, _vp, _vp, _int, _i64, _i64, _vp,
+         _i64, _i64, _dbl, _dbl, _dbl, _vp],
+    ),
+    "vsr_terrain_derivatives_bands": (
+        _int,
+        [_vp, _int, _int, _i64, _i64, _i64, _i64, _dbl, _dbl, _dbl, _int, _dbl, _vp, _vp, _vp, _int, _i64, _i64,
+         _vp],
+    ),
+    "vsr_convolve_bands": (
+        _int,
+        [_vp, _int, _int, _i64, _i64, _i64, _i64, _c.POINTER(_dbl), _int, _int, _dbl, _int, _vp, _int, _i64, _i64,
+         _int, _vp, _sz, _vp],
     ),
     "vsr_terrain_derivatives": (
         _int,
@@ -93,6 +111,14 @@ SIGNATURES: dict[str, tuple] = {
     "vsr_focal_mean": (
         _int,
         [_vp, _int, _i64, _i64, _i64, _int, _int, _dbl, _int, _vp, _int, _i64, _vp],
+    ),
+    "vsr_focal_stat": (
+        _int,
+        [_vp, _int, _i64, _i64, _i64, _int, _int, _int, _dbl, _int, _vp, _int, _i64, _vp],
+    ),
+    "vsr_focal_stat_bands": (
+        _int,
+        [_vp, _int, _int, _i64, _i64, _i64, _i64, _int, _int, _int, _dbl, _int, _vp, _int, _i64, _i64, _vp],
     ),
 }
 

@@ -13,6 +13,11 @@ raster_hillshade       algebra.py:2778-2818             vsr_horn_fused
 raster_convolve        algebra.py:2101-2117             vsr_convolve
 raster_gaussian_filter algebra.py:2120-2154             vsr_gaussian
 raster_focal_mean      algebra.py:3582-3604             vsr_focal_mean
+raster_focal_min       algebra.py:3531-3554             vsr_focal_stat_bands
+raster_focal_max       algebra.py:3557-3579             vsr_focal_stat_bands
+raster_focal_std       algebra.py:3607-3631             vsr_focal_stat_bands
+raster_focal_range     algebra.py:3634-3656             vsr_focal_stat_bands
+raster_focal_variety   algebra.py:3659-3684             vsr_focal_stat_bands
 =====================  ==============================  ==========================
 
 ``raster_terrain`` is new: slope, aspect and hillshade from ONE pass over the
@@ -119,6 +124,15 @@ def _shape_like(raster: OwnedRasterArray, t):
     return t[0] if raster.data.ndim == 2 else t
 
 
+def _shared_layout(*tensors) -> tuple[int, int]:
+    """(band stride, row pitch) in elements shared by the given (B, H, W)
+    output tensors (None entries skipped); rows must be contiguous."""
+    lay = {(t.stride(0), t.stride(1)) for t in tensors if t is not None}
+    if any(t.stride(2) != 1 for t in tensors if t is not None) or len(lay) > 1:
+        raise ValueError("output tensors must share one (band, row) layout with contiguous rows")
+    return lay.pop() if lay else (0, 0)
+
+
 def _record(result: OwnedRasterArray, detail: str, elapsed: float = 0.0) -> OwnedRasterArray:
     result.diagnostics.append(
         RasterDiagnosticEvent(
@@ -160,7 +174,7 @@ def horn_fused(
     nodata_mode: str = NODATA_WINDOW,
     out=None,
 ):
-    """Launch vsr_horn_fused over every band; returns (slope, aspect, hs) tensors.
+    """One vsr_horn_fused_bands launch over every band; returns (slope, aspect, hs) tensors.
 
     ``out`` may supply preallocated (B, H, W) device tensors for the three
     outputs (None entries are allocated).
@@ -190,17 +204,17 @@ def horn_fused(
     code = _lib.dtype_code(dt)
     ocode = _lib.VSR_F64 if compute_np == np.float64 else _lib.VSR_F32
     stream = _stream_handle()
-    esz = src.element_size()
-    for b in range(B):
-        st = lib.vsr_horn_fused(
-            src.data_ptr() + b * H * W * esz, code, H, W, W, cx, cy, ndv, kind, flags,
-            s_t[b].data_ptr() if s_t is not None else None,
-            a_t[b].data_ptr() if a_t is not None else None,
-            ocode, W,
-            h_t[b].data_ptr() if h_t is not None else None, W,
-            float(z_factor), zen, az, stream,
-        )
-        _lib.check(st, "vsr_horn_fused")
+    sa_bs, sa_p = _shared_layout(s_t, a_t)
+    h_bs, h_p = _shared_layout(h_t)
+    st = lib.vsr_horn_fused_bands(
+        src.data_ptr(), code, B, H * W, H, W, W, cx, cy, ndv, kind, flags,
+        s_t.data_ptr() if s_t is not None else None,
+        a_t.data_ptr() if a_t is not None else None,
+        ocode, sa_bs, sa_p,
+        h_t.data_ptr() if h_t is not None else None, h_bs, h_p,
+        float(z_factor), zen, az, stream,
+    )
+    _lib.check(st, "vsr_horn_fused_bands")
     if out_np not in (np.dtype(np.float32), np.dtype(np.float64)):
         s_t = s_t.to(torch_dtype(out_np)) if s_t is not None else None
         a_t = a_t.to(torch_dtype(out_np)) if a_t is not None else None
@@ -288,7 +302,7 @@ def derivative_nodata(dem: OwnedRasterArray) -> float:
 
 def terrain_derivatives(dem: OwnedRasterArray, *, tri: bool = True, tpi: bool = True, curvature: bool = True,
                         out_dtype=np.float64, out=None):
-    """Launch vsr_terrain_derivatives over every band; returns (tri, tpi, curvature) (B, H, W) tensors.
+    """One vsr_terrain_derivatives_bands launch over every band; returns (tri, tpi, curvature) (B, H, W) tensors.
 
     ``out`` may supply preallocated device tensors (None entries are allocated).
     """
@@ -304,17 +318,16 @@ def terrain_derivatives(dem: OwnedRasterArray, *, tri: bool = True, tpi: bool = 
     cx, cy = cellsize(dem.affine)
     lib = _lib.load()
     stream = _stream_handle()
-    esz = src.element_size()
-    for b in range(B):
-        st = lib.vsr_terrain_derivatives(
-            src.data_ptr() + b * H * W * esz, _lib.dtype_code(dt), H, W, W, cx, cy, ndv, kind,
-            derivative_nodata(dem),
-            t_t[b].data_ptr() if t_t is not None else None,
-            p_t[b].data_ptr() if p_t is not None else None,
-            c_t[b].data_ptr() if c_t is not None else None,
-            ocode, W, stream,
-        )
-        _lib.check(st, "vsr_terrain_derivatives")
+    o_bs, o_p = _shared_layout(t_t, p_t, c_t)
+    st = lib.vsr_terrain_derivatives_bands(
+        src.data_ptr(), _lib.dtype_code(dt), B, H * W, H, W, W, cx, cy, ndv, kind,
+        derivative_nodata(dem),
+        t_t.data_ptr() if t_t is not None else None,
+        p_t.data_ptr() if p_t is not None else None,
+        c_t.data_ptr() if c_t is not None else None,
+        ocode, o_bs, o_p, stream,
+    )
+    _lib.check(st, "vsr_terrain_derivatives_bands")
     return t_t, p_t, c_t
 
 
@@ -383,7 +396,7 @@ def _aligned_ptr(t, align: int = 256) -> int:
 
 def convolve_bands(raster: OwnedRasterArray, kernel: np.ndarray, *, precision: str = "auto",
                    out_dtype=np.float64, out=None):
-    """vsr_convolve over every band; returns a (B, H, W) device tensor."""
+    """One vsr_convolve_bands launch over every band; returns a (B, H, W) device tensor."""
     torch = _torch()
     src, dt = _device_bands(raster)
     B, H, W = src.shape
@@ -398,13 +411,11 @@ def convolve_bands(raster: OwnedRasterArray, kernel: np.ndarray, *, precision: s
     ws = _workspace(nbytes, src.device)
     w = np.ascontiguousarray(kernel, dtype=np.float64)
     wp = w.ctypes.data_as(_lib._c.POINTER(_lib._c.c_double))
-    stream = _stream_handle()
-    esz, osz = src.element_size(), dst.element_size()
-    for b in range(B):
-        st = lib.vsr_convolve(src.data_ptr() + b * H * W * esz, _lib.dtype_code(dt), H, W, W, wp, kh, kw,
-                              nd_out if kind == _lib.VSR_NODATA_VALUE else ndv, kind,
-                              dst.data_ptr() + b * H * W * osz, ocode, W, prec, _aligned_ptr(ws), nbytes, stream)
-        _lib.check(st, "vsr_convolve")
+    o_bs, o_p = _shared_layout(dst)
+    st = lib.vsr_convolve_bands(src.data_ptr(), _lib.dtype_code(dt), B, H * W, H, W, W, wp, kh, kw,
+                                nd_out if kind == _lib.VSR_NODATA_VALUE else ndv, kind, dst.data_ptr(), ocode,
+                                o_bs, o_p, prec, _aligned_ptr(ws), nbytes, _stream_handle())
+    _lib.check(st, "vsr_convolve_bands")
     return dst
 
 
@@ -509,3 +520,62 @@ def raster_focal_mean(raster: OwnedRasterArray, radius=1, *, use_gpu: bool | Non
     out = focal_mean_bands(raster, ry, rx, out_dtype=out_dtype)
     res = from_device(_shape_like(raster, out), nodata=raster.nodata, affine=raster.affine, crs=raster.crs)
     return _record(res, f"gpu_focal_mean {raster.width}x{raster.height} radius=({ry},{rx})", time.perf_counter() - t0)
+
+
+def focal_stat_bands(raster: OwnedRasterArray, stat: str, ry: int, rx: int, *, out_dtype=np.float64, out=None):
+    """One focal statistic over every band in one launch; (B, H, W) device tensor."""
+    torch = _torch()
+    if stat not in _lib.VSR_STAT:
+        raise ValueError(f"unknown focal statistic {stat!r}; expected one of {sorted(_lib.VSR_STAT)}")
+    src, dt = _device_bands(raster)
+    B, H, W = src.shape
+    kind, ndv = nodata_kind(raster)
+    nd_out = float(raster.nodata) if raster.nodata is not None else 0.0
+    ocode, odt = _out_code(out_dtype)
+    dst = out if out is not None else torch.empty((B, H, W), dtype=torch_dtype(odt), device=src.device)
+    lib = _lib.load()
+    st = lib.vsr_focal_stat_bands(src.data_ptr(), _lib.dtype_code(dt), B, H * W, H, W, W, _lib.VSR_STAT[stat], ry, rx,
+                                  nd_out if kind == _lib.VSR_NODATA_VALUE else ndv, kind, dst.data_ptr(), ocode,
+                                  H * W, W, _stream_handle())
+    _lib.check(st, "vsr_focal_stat_bands")
+    return dst
+
+
+def _raster_focal(raster: OwnedRasterArray, stat: str, radius, use_gpu, out_dtype) -> OwnedRasterArray:
+    ry, rx = _parse_radius(radius)
+    _require_gpu(use_gpu)
+    t0 = time.perf_counter()
+    out = focal_stat_bands(raster, stat, ry, rx, out_dtype=out_dtype)
+    res = from_device(_shape_like(raster, out), nodata=raster.nodata, affine=raster.affine, crs=raster.crs)
+    return _record(res, f"gpu_focal_{stat} {raster.width}x{raster.height} radius=({ry},{rx})",
+                   time.perf_counter() - t0)
+
+
+def raster_focal_min(raster: OwnedRasterArray, radius=1, *, use_gpu: bool | None = None,
+                     out_dtype=np.float64) -> OwnedRasterArray:
+    """Focal minimum, reference algebra.py:3531-3554 (CPU semantics :3041-3059)."""
+    return _raster_focal(raster, "min", radius, use_gpu, out_dtype)
+
+
+def raster_focal_max(raster: OwnedRasterArray, radius=1, *, use_gpu: bool | None = None,
+                     out_dtype=np.float64) -> OwnedRasterArray:
+    """Focal maximum, reference algebra.py:3557-3579 (CPU semantics :3062-3081)."""
+    return _raster_focal(raster, "max", radius, use_gpu, out_dtype)
+
+
+def raster_focal_std(raster: OwnedRasterArray, radius=1, *, use_gpu: bool | None = None,
+                     out_dtype=np.float64) -> OwnedRasterArray:
+    """Focal population standard deviation, reference algebra.py:3607-3631 (:3104-3122)."""
+    return _raster_focal(raster, "std", radius, use_gpu, out_dtype)
+
+
+def raster_focal_range(raster: OwnedRasterArray, radius=1, *, use_gpu: bool | None = None,
+                       out_dtype=np.float64) -> OwnedRasterArray:
+    """Focal range (max - min), reference algebra.py:3634-3656 (:3125-3143)."""
+    return _raster_focal(raster, "range", radius, use_gpu, out_dtype)
+
+
+def raster_focal_variety(raster: OwnedRasterArray, radius=1, *, use_gpu: bool | None = None,
+                         out_dtype=np.float64) -> OwnedRasterArray:
+    """Number of distinct values in the window, reference algebra.py:3659-3684 (:3146-3163)."""
+    return _raster_focal(raster, "variety", radius, use_gpu, out_dtype)
