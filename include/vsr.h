@@ -69,10 +69,18 @@ extern "C" {
  * algebra.py:2188-2189).  Hillshade always masks. */
 #define VSR_HORN_SA_NAN_UNMASKED 2u
 
-/* ---- precision for focal convolution ----------------------------------- */
-#define VSR_PREC_AUTO 0       /* split-BF16 tensor cores for k >= 15, else FP32 */
-#define VSR_PREC_FP32 1       /* FP32 CUDA-core direct / separable kernels      */
-#define VSR_PREC_SPLIT_BF16 2 /* tcgen05 implicit GEMM, hi/lo BF16, FP32 accum  */
+/* ---- precision for focal convolution -----------------------------------
+ * VSR_PREC_SPLIT runs tcgen05 tensor-core GEMMs on split operands with FP32
+ * accumulation (hi*hi + hi*lo + lo*hi).  The high parts are BF16; the low
+ * part of the data is F16 (11 more bits than BF16, so the dropped lo*lo term
+ * is ~2^-20 of a product instead of ~2^-18): the convolution pairs it with
+ * an F16 copy of the whole weight, the Gaussian line passes split both sides
+ * into F16 pairs.  The two operands of each MMA share one type.
+ * VSR_PREC_SPLIT_BF16 is the same code under the name the first builds used. */
+#define VSR_PREC_AUTO 0       /* split tensor cores where they pay, else FP32  */
+#define VSR_PREC_FP32 1       /* FP32 CUDA-core direct / separable kernels     */
+#define VSR_PREC_SPLIT 2      /* tcgen05 split-precision GEMM, FP32 accumulate */
+#define VSR_PREC_SPLIT_BF16 VSR_PREC_SPLIT
 
 /* ---- library ------------------------------------------------------------ */
 VSR_API int vsr_version(void);                 /* major*10000 + minor*100 + patch      */
@@ -214,7 +222,7 @@ VSR_API int vsr_convolve_bands(const void* src, int dtype, int bands, int64_t ba
  * through a plugin boundary (ctypes / cgo / JNI) with no access to the
  * process's device allocator.  Same arguments and results as vsr_convolve
  * without the workspace: the scratch is a static device array inside libvsr
- * (248,320 bytes, enough for every kernel up to 80 x 80 at any precision;
+ * (358,912 bytes, enough for every kernel up to 80 x 80 at any precision;
  * every GPU that loads the library holds it until the process exits).
  * Larger kernels are rejected with VSR_ERR_UNSUPPORTED.  The first call on
  * each device resolves the array's device address (with that device
@@ -238,7 +246,7 @@ VSR_API int vsr_convolve_noalloc(const void* src, int dtype, int64_t height, int
  * sizes are bumped to odd.  Same output rule as vsr_convolve.
  *
  * precision: VSR_PREC_FP32 runs the separable FP32 CUDA-core kernels.
- * VSR_PREC_SPLIT_BF16 runs the two line passes on the tcgen05 tensor cores
+ * VSR_PREC_SPLIT runs the two line passes on the tcgen05 tensor cores
  * (8/16-bit integer rasters, kernel_size <= 79): each a GEMM against the
  * Toeplitz band of the split weights (hi*hi + hi*lo + lo*hi, FP32
  * accumulation), the row pass's sums kept as two float32 planes in the

@@ -137,12 +137,12 @@ def test_ctypes_signatures_match_the_header():
 
 
 def test_noalloc_scratch_covers_every_supported_kernel(lib):
-    """vsr_convolve_noalloc's static scratch (248,320 bytes) holds the workspace
+    """vsr_convolve_noalloc's static scratch (358,912 bytes) holds the workspace
     vsr_convolve asks for at every precision for every kernel up to 80 x 80
     (host-only size queries), and the split-BF16 41 x 41 case fills it exactly."""
     from vsr_gb300 import _lib
 
-    limit = 248320
+    limit = 358912
     for kh in range(1, 81):
         for kw in range(1, 81):
             for prec in (_lib.VSR_PREC_AUTO, _lib.VSR_PREC_FP32, _lib.VSR_PREC_SPLIT_BF16):

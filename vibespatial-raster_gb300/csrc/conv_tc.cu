@@ -19,12 +19,20 @@
 // taps of K per N outputs) N = 64 and N = 128 cost the same per output and
 // N = 64 needs half the shared memory.
 //
-// Precision: values are centred on the tile's centre pixel (mu) and split
-// z = z_hi + z_lo, w = w_hi + w_lo (BF16).  The hi*hi chain accumulates in
-// FP32 tensor memory in groups of kernel rows (the accumulation error grows
-// with the number of MMAs chained into one accumulator), the two correction
-// products (hi*lo, lo*hi) in one more accumulator; the groups are added in
-// FP32 registers.  The weight sum uses the same split weights, so the
+// Precision: values are centred on the tile's centre pixel (mu), scaled by
+// a power of two zs (from the raster's largest finite value, so that
+// |z| < 2^15) and split z = z_hi + z_lo with z_hi BF16 and z_lo F16; the
+// weights, scaled by a power of two ws (largest |w| near 2^13), are split
+// w = w_hi + w_lo (BF16) and also kept as w16 = F16(w_hi + w_lo).  Three
+// products per tap: z_hi*w_hi and z_hi*w_lo (BF16 MMAs) and z_lo*w16 (an F16
+// MMA; each MMA's two operands share a type).  The F16 low part carries 11
+// more bits of z than a BF16 one would, and pairing it with a full-precision
+// weight leaves out only z_lo * (w - w16), about 2^-20 of a product, where a
+// BF16 pair leaves out z_lo * w_lo, about 2^-18.  The hi*hi chain
+// accumulates in FP32 tensor memory in groups of kernel rows (the
+// accumulation error grows with the number of MMAs chained into one
+// accumulator), the two correction products in one more accumulator; the
+// groups are added in FP32 registers and the sum is scaled back by 1/zs.  The weight sum uses the same split weights, so the
 // quotient is a consistently weighted mean: on tiles whose window holds no
 // nodata it comes from a summed-area table of w_hi + w_lo (borders only
 // clip the window), otherwise from a 0/1 validity operand times w_hi and
@@ -102,7 +110,7 @@ __host__ __device__ inline TcGeom make_geom(int kh, int kw) {
 struct TcPlan {  // shared-memory byte offsets (1024-aligned base) and pipeline shape
   uint32_t a_bytes;             // one operand buffer
   uint32_t a_hi, a_lo, a_vd;    // nbuf buffers each
-  uint32_t ring;                // nst stages of kRowsPerStage x (hi band, lo band)
+  uint32_t ring;                // nst stages of kRowsPerStage x (hi, lo, f16 band)
   uint32_t row_bytes, stage_bytes;
   uint32_t sat;                 // (kh+1) x (kw+1) doubles
   uint32_t ctr;                 // 2 x kM u64 centre-validity bits
@@ -125,7 +133,7 @@ __host__ __device__ inline TcPlan make_plan(const TcGeom& g, bool has_nd, int nb
   p.a_lo = p.a_hi + nbuf * p.a_bytes;
   p.a_vd = p.a_lo + nbuf * p.a_bytes;
   p.ring = p.a_vd + (has_nd ? nbuf * p.a_bytes : 0u);
-  p.row_bytes = 2u * g.NB * 128;
+  p.row_bytes = 3u * g.NB * 128;
   p.stage_bytes = kRowsPerStage * p.row_bytes;
   p.sat = p.ring + nst * p.stage_bytes;
   p.ctr = (p.sat + static_cast<uint32_t>(g.kh + 1) * (g.kw + 1) * 8 + 127) & ~127u;
@@ -179,8 +187,9 @@ struct TcArgs {
   int out_dtype;
   int64_t out_pitch;
   int vec_out;                  // float32 output with 16-byte aligned rows
-  const unsigned char* bw_img;  // per kernel row: hi band, lo band (NB core matrices each)
-  const double* sat;            // (kh+1) x (kw+1) prefix sums of w_hi + w_lo
+  const unsigned char* bw_img;  // per kernel row: hi, lo (BF16) and w16 (F16) bands, NB core matrices each
+  const double* sat;            // (kh+1) x (kw+1) prefix sums of w_hi + w_lo (scaled by ws)
+  const uint32_t* vmax_bits;    // largest finite |value| of the raster (float bits), sets zs
   const double* w64;            // the kernel as given (windows holding +-inf)
   int kh, kw;
   int nbuf, nst;
@@ -234,6 +243,17 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
   const TcGeom g = make_geom(a.kh, a.kw);
   const TcPlan L = make_plan(g, ND != 0, a.nbuf, a.nst);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // value scale zs = 2^(14 - E) for a largest |value| below 2^E: |v - mu| < 2^15
+  int zexp = 0;
+  {
+    const float vmax = __uint_as_float(*a.vmax_bits);
+    if (vmax > 0.0f && isfinite(vmax)) {
+      int e = 0;
+      frexpf(vmax, &e);
+      zexp = max(-120, min(120, 14 - e));
+    }
+  }
+  const float zs = ldexpf(1.0f, zexp), unscale = ldexpf(1.0f, -zexp);
   const int64_t tiles_x = (a.W + kTN - 1) / kTN;
   const int64_t per_band = tiles_x * ((a.H + kM - 1) / kM);
   const int64_t total = per_band * a.bands;
@@ -309,10 +329,10 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
             // A_ky = the window advanced ky rows (16 bytes each); one k-step =
             // two core matrices along K on both operands
             uint32_t ah = w_ahi + ky, al = w_alo + ky, av = w_avd + ky;
-            uint32_t bh = w_ring + s * stage_w + (ky - ky0) * row_w, bl = bh + g.NB * 8;
+            uint32_t bh = w_ring + s * stage_w + (ky - ky0) * row_w, bl = bh + g.NB * 8, bf = bh + 2 * g.NB * 8;
             mma_bf16(tg, ah, bh, f);
             mma_bf16(t_corr, ah, bl, ky != 0);
-            mma_bf16(t_corr, al, bh, 1u);
+            mma_f16(t_corr, al, bf, 1u);
             if (den_mma) {
               mma_bf16(td, av, bh, f);
               mma_bf16(td, av, bl, 1u);
@@ -323,9 +343,10 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
                 av += a_ks;
                 bh += 16;
                 bl += 16;
+                bf += 16;
                 mma_bf16(tg, ah, bh, 1u);
                 mma_bf16(t_corr, ah, bl, 1u);
-                mma_bf16(t_corr, al, bh, 1u);
+                mma_f16(t_corr, al, bf, 1u);
                 mma_bf16(td, av, bh, 1u);
                 mma_bf16(td, av, bl, 1u);
               }
@@ -336,9 +357,10 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
                 al += a_ks;
                 bh += 16;
                 bl += 16;
+                bf += 16;
                 mma_bf16(tg, ah, bh, 1u);
                 mma_bf16(t_corr, ah, bl, 1u);
-                mma_bf16(t_corr, al, bh, 1u);
+                mma_f16(t_corr, al, bf, 1u);
               }
             }
           }
@@ -390,7 +412,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
     const int kh2 = a.kh / 2, kw2 = a.kw / 2;
     const int S1 = a.kw + 1;
     const float wtot = static_cast<float>(sat[a.kh * S1 + a.kw]);
-    const float inv_wtot = __frcp_rn(wtot);
+    const float inv_wtot = __frcp_rn(wtot) * unscale;
     // this lane's window columns 4*lane .. 4*lane+3; in the K-reversed A
     // layout they are elements klo+3 .. klo of one core-matrix row, so each
     // operand takes one 8-byte store per window row
@@ -481,7 +503,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
           for (int n = 0; n < 16; ++n) {
             const bool nd = !((cb >> n) & 1u) || !(den[n] > 0.0f);
             ndm |= static_cast<uint32_t>(nd) << n;
-            const float inv = (ND == 0 || !den_mma) && interior ? inv_wtot : __frcp_rn(den[n]);
+            const float inv = (ND == 0 || !den_mma) && interior ? inv_wtot : __frcp_rn(den[n]) * unscale;
             num[n] = ((fb >> n) & 1u) ? __int_as_float(0x7fc00000) : fmaf(num[n], inv, mu);
           }
           for (uint32_t r = ib & ~ndm; r; r &= r - 1) {  // windows holding +-inf (rare)
@@ -583,7 +605,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
             const bool inb = (in >> q) & 1u;
             const bool okv = inb && (ND == 1 ? v != a.nd_f : (ND == 2 ? v == v : true));
             const bool fin = fabsf(v) <= 3.402823466e38f;  // false for NaN and +-inf
-            z[q] = (okv && fin) ? v - mu : 0.0f;
+            z[q] = (okv && fin) ? (v - mu) * zs : 0.0f;
             okm |= static_cast<uint32_t>(okv) << q;
             badm |= static_cast<uint32_t>(inb && !fin) << q;
           }
@@ -591,10 +613,10 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
           if (lane_cols) {
             const __nv_bfloat162 h32 = __floats2bfloat162_rn(z[3], z[2]);
             const __nv_bfloat162 h10 = __floats2bfloat162_rn(z[1], z[0]);
-            const __nv_bfloat162 l32 = __floats2bfloat162_rn(z[3] - __low2float(h32), z[2] - __high2float(h32));
-            const __nv_bfloat162 l10 = __floats2bfloat162_rn(z[1] - __low2float(h10), z[0] - __high2float(h10));
+            const __half2 l32 = __floats2half2_rn(z[3] - __low2float(h32), z[2] - __high2float(h32));
+            const __half2 l10 = __floats2half2_rn(z[1] - __low2float(h10), z[0] - __high2float(h10));
             *reinterpret_cast<uint2*>(ahi + rho * 16) = make_uint2(bf16x2_bits(h32), bf16x2_bits(h10));
-            *reinterpret_cast<uint2*>(alo + rho * 16) = make_uint2(bf16x2_bits(l32), bf16x2_bits(l10));
+            *reinterpret_cast<uint2*>(alo + rho * 16) = make_uint2(f16x2_bits(l32), f16x2_bits(l10));
             if (ND != 0)
               *reinterpret_cast<uint2*>(avd + rho * 16) =
                   make_uint2(((okm & 8u) ? 0x3f80u : 0u) | ((okm & 4u) ? 0x3f800000u : 0u),
@@ -683,11 +705,11 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
   }
 }
 
-// Toeplitz band images: for kernel row ky, split s in {hi, lo}, core matrix
-// c, row r, element e -> w[ky][Kp-1-8c-e-r] (0 outside [0, kw)), split as
-// w = bf16(w) + bf16(w - bf16(w)); laid out [ky][s][c][r][e] so a kernel
-// row's two bands are one contiguous copy.
-__global__ void prep_tc_weights(const double* __restrict__ w64, int kh, int kw, int Kp, int NB,
+// Toeplitz band images: for kernel row ky, band s, core matrix c, row r,
+// element e -> w'[ky][Kp-1-8c-e-r] (0 outside [0, kw)) with w' = w * ws:
+// s = 0: BF16(w'), s = 1: BF16(w' - hi), s = 2: F16(hi + lo); laid out
+// [ky][s][c][r][e] so a kernel row's three bands are one contiguous copy.
+__global__ void prep_tc_weights(const double* __restrict__ w64, int kh, int kw, int Kp, int NB, double ws,
                                 uint16_t* __restrict__ img) {
   const int per_row = NB * 64;
   const int total = kh * per_row;
@@ -695,23 +717,26 @@ __global__ void prep_tc_weights(const double* __restrict__ w64, int kh, int kw, 
     const int ky = i / per_row, rem = i - ky * per_row;
     const int c = rem / 64, r = (rem / 8) & 7, e = rem & 7;
     const int kx = Kp - 1 - 8 * c - e - r;
-    const double w = (kx >= 0 && kx < kw) ? w64[ky * kw + kx] : 0.0;
+    const double w = (kx >= 0 && kx < kw) ? w64[ky * kw + kx] * ws : 0.0;
     const __nv_bfloat16 hi = __float2bfloat16_rn(static_cast<float>(w));
-    const __nv_bfloat16 lo = __float2bfloat16_rn(static_cast<float>(w - static_cast<double>(__bfloat162float(hi))));
-    img[((ky * 2 + 0) * NB + c) * 64 + r * 8 + e] = __bfloat16_as_ushort(hi);
-    img[((ky * 2 + 1) * NB + c) * 64 + r * 8 + e] = __bfloat16_as_ushort(lo);
+    const double h = static_cast<double>(__bfloat162float(hi));
+    const __nv_bfloat16 lo = __float2bfloat16_rn(static_cast<float>(w - h));
+    const __half w16 = __float2half_rn(static_cast<float>(h + static_cast<double>(__bfloat162float(lo))));
+    img[((ky * 3 + 0) * NB + c) * 64 + r * 8 + e] = __bfloat16_as_ushort(hi);
+    img[((ky * 3 + 1) * NB + c) * 64 + r * 8 + e] = __bfloat16_as_ushort(lo);
+    img[((ky * 3 + 2) * NB + c) * 64 + r * 8 + e] = __half_as_ushort(w16);
   }
 }
 
-// Summed-area table of the split weights w_hi + w_lo in float64:
-// sat[i][j] = sum of w over rows < i and columns < j.  One block: split
+// Summed-area table of the split scaled weights w_hi + w_lo in float64:
+// sat[i][j] = sum of w' over rows < i and columns < j.  One block: split
 // weights to shared memory, row prefix sums (a thread per row), then
 // column sums (a thread per column).
-__global__ void prep_tc_sat(const double* __restrict__ w64, int kh, int kw, double* __restrict__ sat) {
+__global__ void prep_tc_sat(const double* __restrict__ w64, int kh, int kw, double wscale, double* __restrict__ sat) {
   __shared__ double ws[kMaxTCK * kMaxTCK];
   const int tid = threadIdx.x;
   for (int i = tid; i < kh * kw; i += blockDim.x) {
-    const double w = w64[i];
+    const double w = w64[i] * wscale;
     const double h = __bfloat162float(__float2bfloat16_rn(static_cast<float>(w)));
     ws[i] = h + static_cast<double>(__bfloat162float(__float2bfloat16_rn(static_cast<float>(w - h))));
   }
@@ -732,6 +757,40 @@ __global__ void prep_tc_sat(const double* __restrict__ w64, int kh, int kw, doub
       sat[i * (kw + 1) + tid] = acc;
     }
   }
+}
+
+// Largest |v| over the finite, non-nodata values of every band, as float
+// bits (non-negative floats order like their bit patterns), ORed into
+// *out by atomicMax.  Rows are spread over the grid; 16-byte loads when the
+// rows allow.
+__global__ void __launch_bounds__(256) raster_absmax(const float* __restrict__ src, int64_t H, int64_t W,
+                                                     int64_t pitch, int bands, int64_t band_stride, int nd_kind,
+                                                     float nd_f, int vec, uint32_t* __restrict__ out) {
+  float m = 0.0f;
+  auto take = [&](float v) {
+    const bool ok = isfinite(v) && !(nd_kind == VSR_NODATA_VALUE && v == nd_f);
+    m = ok ? fmaxf(m, fabsf(v)) : m;
+  };
+  const int64_t rows = static_cast<int64_t>(bands) * H;
+  for (int64_t rr = blockIdx.x; rr < rows; rr += gridDim.x) {
+    const int64_t b = rr / H, y = rr - b * H;
+    const float* row = src + b * band_stride + y * pitch;
+    int64_t x0 = 0;
+    if (vec) {
+      const int64_t n4 = W / 4;
+      for (int64_t i = threadIdx.x; i < n4; i += blockDim.x) {
+        const float4 q = __ldg(reinterpret_cast<const float4*>(row) + i);
+        take(q.x);
+        take(q.y);
+        take(q.z);
+        take(q.w);
+      }
+      x0 = n4 * 4;
+    }
+    for (int64_t x = x0 + threadIdx.x; x < W; x += blockDim.x) take(__ldg(row + x));
+  }
+  for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(out, __float_as_uint(m));
 }
 
 }  // namespace
@@ -760,21 +819,22 @@ int conv_tc_supported(int kh, int kw) {
   return p.total <= kSmemLimit && g.KW <= 128 && p.cols <= 512;
 }
 
-// Workspace: float64 weights | Toeplitz band images | summed-area table.
+// Workspace: float64 weights | Toeplitz band images | summed-area table |
+// the largest |value| word (256 bytes).
 size_t conv_tc_workspace(int kh, int kw) {
   const TcGeom g = make_geom(kh, kw);
   const size_t a = (static_cast<size_t>(kh) * kw * 8 + 255) & ~size_t(255);
-  const size_t b = (static_cast<size_t>(kh) * 2 * g.NB * 128 + 255) & ~size_t(255);
+  const size_t b = (static_cast<size_t>(kh) * 3 * g.NB * 128 + 255) & ~size_t(255);
   const size_t c = (static_cast<size_t>(kh + 1) * (kw + 1) * 8 + 255) & ~size_t(255);
-  return a + b + c;
+  return a + b + c + 256;
 }
 
 int run_conv_tc(const void* src, int dtype, int bands, int64_t band_stride, int64_t H, int64_t W, int64_t pitch,
                 const double* weights_host, int kh, int kw, double nodata, int nodata_kind, void* dst, int out_dtype,
                 int64_t out_band_stride, int64_t out_pitch, void* workspace, size_t ws_bytes, cudaStream_t st) {
-  if (dtype != VSR_F32) return fail(VSR_ERR_UNSUPPORTED, "split-BF16 convolution reads float32 rasters");
+  if (dtype != VSR_F32) return fail(VSR_ERR_UNSUPPORTED, "split-precision convolution reads float32 rasters");
   if (!conv_tc_supported(kh, kw))
-    return fail(VSR_ERR_UNSUPPORTED, "split-BF16 convolution supports kernels up to %dx%d", kMaxTCK, kMaxTCK);
+    return fail(VSR_ERR_UNSUPPORTED, "split-precision convolution supports kernels up to %dx%d", kMaxTCK, kMaxTCK);
   const size_t need = conv_tc_workspace(kh, kw);
   if (!workspace || ws_bytes < need || !aligned(workspace, 256))
     return fail(VSR_ERR_WORKSPACE, "workspace must be 256-byte aligned and >= %zu bytes", need);
@@ -784,25 +844,44 @@ int run_conv_tc(const void* src, int dtype, int bands, int64_t band_stride, int6
   const bool has_nd = kind != VSR_NODATA_NONE;
   int nbuf = 0, nst = 0;
   tc_shape(kh, kw, has_nd, &nbuf, &nst);
-  if (!nbuf) return fail(VSR_ERR_UNSUPPORTED, "split-BF16 convolution: %dx%d kernel does not fit shared memory", kh, kw);
+  if (!nbuf) return fail(VSR_ERR_UNSUPPORTED, "split-precision convolution: %dx%d kernel does not fit shared memory", kh, kw);
   const TcPlan L = make_plan(g, has_nd, nbuf, nst);
   char* ws = static_cast<char*>(workspace);
   double* w64 = reinterpret_cast<double*>(ws);
   const size_t off_img = (static_cast<size_t>(kh) * kw * 8 + 255) & ~size_t(255);
-  const size_t off_sat = off_img + ((static_cast<size_t>(kh) * 2 * g.NB * 128 + 255) & ~size_t(255));
+  const size_t off_sat = off_img + ((static_cast<size_t>(kh) * 3 * g.NB * 128 + 255) & ~size_t(255));
+  const size_t off_vmax = off_sat + ((static_cast<size_t>(kh + 1) * (kw + 1) * 8 + 255) & ~size_t(255));
   uint16_t* img = reinterpret_cast<uint16_t*>(ws + off_img);
   double* sat = reinterpret_cast<double*>(ws + off_sat);
+  uint32_t* vmax = reinterpret_cast<uint32_t*>(ws + off_vmax);
+  // weight scale: a power of two bringing the largest |w| to [2^12, 2^13)
+  double wmax = 0.0;
+  for (int i = 0; i < kh * kw; ++i)
+    if (std::isfinite(weights_host[i])) wmax = std::max(wmax, std::fabs(weights_host[i]));
+  int we = 0;
+  if (wmax > 0.0) std::frexp(wmax, &we);
+  const double wscale = wmax > 0.0 ? std::ldexp(1.0, std::max(-900, std::min(900, 13 - we))) : 1.0;
   VSR_CUDA_TRY(cudaMemcpyAsync(w64, weights_host, static_cast<size_t>(kh) * kw * 8, cudaMemcpyHostToDevice, st));
-  prep_tc_weights<<<16, 256, 0, st>>>(w64, kh, kw, g.Kp, g.NB, img);
+  prep_tc_weights<<<16, 256, 0, st>>>(w64, kh, kw, g.Kp, g.NB, wscale, img);
   VSR_CUDA_TRY(cudaGetLastError());
-  prep_tc_sat<<<1, 64, 0, st>>>(w64, kh, kw, sat);
+  prep_tc_sat<<<1, 64, 0, st>>>(w64, kh, kw, wscale, sat);
   VSR_CUDA_TRY(cudaGetLastError());
+  VSR_CUDA_TRY(cudaMemsetAsync(vmax, 0, sizeof(uint32_t), st));
+  {
+    const bool vec = aligned(src, 16) && pitch % 4 == 0 && (bands == 1 || band_stride % 4 == 0);
+    const int64_t rows = static_cast<int64_t>(bands) * H;
+    const int blocks = static_cast<int>(std::min<int64_t>(rows, static_cast<int64_t>(sm_count()) * 8));
+    raster_absmax<<<blocks, 256, 0, st>>>(static_cast<const float*>(src), H, W, pitch, bands,
+                                          bands > 1 ? band_stride : 0, kind, static_cast<float>(ndv), vec ? 1 : 0,
+                                          vmax);
+    VSR_CUDA_TRY(cudaGetLastError());
+  }
   uint32_t* err = device_error_word();
   if (!err) return VSR_ERR_CUDA;
   const bool vec_out =
       out_dtype == VSR_F32 && aligned(dst, 16) && out_pitch % 4 == 0 && (bands == 1 || out_band_stride % 4 == 0);
   TcArgs a{static_cast<const float*>(src), H, W, pitch, kind, static_cast<float>(ndv), nodata, dst, out_dtype,
-           out_pitch, vec_out ? 1 : 0, reinterpret_cast<const unsigned char*>(img), sat, w64, kh, kw, nbuf, nst,
+           out_pitch, vec_out ? 1 : 0, reinterpret_cast<const unsigned char*>(img), sat, vmax, w64, kh, kw, nbuf, nst,
            bands, bands > 1 ? band_stride : 0, bands > 1 ? out_band_stride : 0};
   // At least 116 KB of shared memory keeps one CTA (and its 512 TMEM columns) per SM.
   const size_t smem = std::max<size_t>(L.total + 1024, 116 * 1024);

@@ -1281,16 +1281,16 @@ extern "C" int vsr_convolve_bands(const void* src, int dtype, int bands, int64_t
     return fail(VSR_ERR_INVALID_ARG, "band strides smaller than one band");
   if (!weights_host) return fail(VSR_ERR_INVALID_ARG, "weights_host is NULL");
   if (kh <= 0 || kw <= 0) return fail(VSR_ERR_INVALID_ARG, "kernel must be at least 1 x 1");
-  if (precision < VSR_PREC_AUTO || precision > VSR_PREC_SPLIT_BF16) return fail(VSR_ERR_INVALID_ARG, "bad precision %d", precision);
+  if (precision < VSR_PREC_AUTO || precision > VSR_PREC_SPLIT) return fail(VSR_ERR_INVALID_ARG, "bad precision %d", precision);
   if (kh > kMaxDirectK || kw > kMaxDirectK)
     return fail(VSR_ERR_UNSUPPORTED, "kernel %dx%d larger than the supported %dx%d", kh, kw, kMaxDirectK, kMaxDirectK);
   // Tensor-core path: float32 rasters and kernels that fit its shared-memory
   // plan.  AUTO takes it for k >= 15 on both axes when the kernel is well
-  // conditioned: split-BF16 weights carry 16 mantissa bits, and a weight sum
+  // conditioned: split weights carry 16 mantissa bits, and a weight sum
   // that nearly cancels (sum |w| > 4 |sum w|) would amplify that rounding.
   const bool tc_ok = dtype == VSR_F32 && conv_tc_supported(kh, kw) && aligned(src, 4);
-  if (precision == VSR_PREC_SPLIT_BF16 && !tc_ok)
-    return fail(VSR_ERR_UNSUPPORTED, "split-BF16 convolution needs a float32 raster and a kernel of at most 41x41");
+  if (precision == VSR_PREC_SPLIT && !tc_ok)
+    return fail(VSR_ERR_UNSUPPORTED, "split-precision convolution needs a float32 raster and a kernel of at most 41x41");
   bool well_conditioned = false;
   if (precision == VSR_PREC_AUTO && tc_ok && kh >= 15 && kw >= 15) {
     double s = 0.0, sa = 0.0;
@@ -1300,7 +1300,7 @@ extern "C" int vsr_convolve_bands(const void* src, int dtype, int bands, int64_t
     }
     well_conditioned = sa <= 4.0 * std::fabs(s);
   }
-  if (precision == VSR_PREC_SPLIT_BF16 || well_conditioned)
+  if (precision == VSR_PREC_SPLIT || well_conditioned)
     return run_conv_tc(src, dtype, bands, band_stride, height, width, pitch, weights_host, kh, kw, nodata,
                        nodata_kind, dst, out_dtype, out_band_stride, out_pitch, workspace, workspace_bytes,
                        static_cast<cudaStream_t>(stream));
@@ -1350,7 +1350,7 @@ extern "C" size_t vsr_gaussian_workspace_size(int kernel_size, int precision) {
   return gauss_ws(k);
 }
 
-// VSR_PREC_AUTO takes the split-BF16 line passes where the separable FP32
+// VSR_PREC_AUTO takes the split-precision line passes where the separable FP32
 // kernels would use the strip kernel (k > 33) on an 8/16-bit integer raster
 // (exact BF16 hi/lo values) and the caller's workspace holds their planes.
 static bool gauss_tc_auto(int dtype, int64_t height, int64_t width, int k, const void* workspace, size_t bytes) {
@@ -1363,7 +1363,7 @@ extern "C" size_t vsr_gaussian_workspace_bytes(int64_t height, int64_t width, in
   if (!(sigma > 0.0) || height < 0 || width < 0) return 0;
   const int k = gaussian_size(sigma, kernel_size);
   const bool tc = gauss_tc_supported(dtype, k) &&
-                  (precision == VSR_PREC_SPLIT_BF16 || (precision == VSR_PREC_AUTO && k > kMaxSepK));
+                  (precision == VSR_PREC_SPLIT || (precision == VSR_PREC_AUTO && k > kMaxSepK));
   return tc ? std::max(gauss_ws(k), gauss_tc_workspace(height, width, dtype, k)) : gauss_ws(k);
 }
 
@@ -1375,10 +1375,10 @@ static int gaussian_impl(const void* src, int dtype, int bands, int64_t band_str
   if (bands < 1) return fail(VSR_ERR_INVALID_ARG, "bands must be >= 1");
   int rc = check_raster(src, dtype, height, width, pitch, dst, out_dtype, out_pitch);
   if (rc || height == 0 || width == 0) return rc;
-  if (precision < VSR_PREC_AUTO || precision > VSR_PREC_SPLIT_BF16) return fail(VSR_ERR_INVALID_ARG, "bad precision %d", precision);
+  if (precision < VSR_PREC_AUTO || precision > VSR_PREC_SPLIT) return fail(VSR_ERR_INVALID_ARG, "bad precision %d", precision);
   const int k = gaussian_size(sigma, kernel_size);
   if (k > kMaxDirectK) return fail(VSR_ERR_UNSUPPORTED, "Gaussian kernel %d larger than %d", k, kMaxDirectK);
-  if (precision == VSR_PREC_SPLIT_BF16 || gauss_tc_auto(dtype, height, width, k, workspace, workspace_bytes))
+  if (precision == VSR_PREC_SPLIT || gauss_tc_auto(dtype, height, width, k, workspace, workspace_bytes))
     return run_gauss_tc(src, dtype, bands, band_stride, height, width, pitch, sigma, k, nodata, nodata_kind, dst,
                         out_dtype, out_band_stride, out_pitch, workspace, workspace_bytes,
                         static_cast<cudaStream_t>(stream));

@@ -6,19 +6,20 @@
 // when it started, or a host that reaches this library through a plugin
 // boundary (ctypes / cgo / JNI) with no access to the process's device
 // allocator.  For them this entry point takes only the inputs and the output;
-// its scratch (the staged float64 weights and the float32 or BF16 operand
-// images built from them) lives in a file-scope __device__ array sized for the
-// largest supported kernel of either precision.  Every GPU that loads the
-// library holds that array (kNoAllocScratchBytes, 242.5 KiB) until the process
-// exits.
+// its scratch (the staged float64 weights, the float32 or split-precision
+// operand images built from them, and the tensor-core path's largest-value
+// word) lives in a file-scope __device__ array sized for the largest
+// supported kernel of either precision.  Every GPU that loads the library
+// holds that array (kNoAllocScratchBytes, 350.5 KiB) until the process exits.
 //
 // Host code cannot use the array's name as a device address, so on the first
 // call on each device (with that device current) the address is resolved
 // with cudaGetSymbolAddress and cached; make that first call before any
 // stream capture.  All calls share the one array and it keeps the last
-// call's contents (each call rewrites every byte it reads, so nothing needs
-// clearing); calls whose kernels overlap on the GPU -- e.g. on two streams
-// at once -- race on it.
+// call's contents: each call rewrites every byte it reads, and the one word
+// that must start at zero (the tensor-core path's largest |value|) is
+// cleared by a cudaMemsetAsync on the caller's stream.  Calls whose kernels
+// overlap on the GPU -- e.g. on two streams at once -- race on it.
 #include <mutex>
 
 #include "vsr_internal.cuh"
@@ -31,9 +32,11 @@ constexpr int kNoAllocMaxK = 80;
 // The larger of the two workspaces vsr_convolve can ask for:
 //  * FP32 path, 80 x 80: 51,200 B float64 weights + 25,600 B float32 rows +
 //    256 B for the total = 77,056 B;
-//  * split-BF16 path, 41 x 41: 13,568 B float64 weights + 220,416 B Toeplitz
-//    band images + 14,336 B float64 summed-area table = 248,320 B.
-constexpr size_t kNoAllocScratchBytes = 248320;
+//  * tensor-core path, 41 x 41: 13,568 B float64 weights + 330,752 B
+//    Toeplitz band images (three bands of 21 core matrices per kernel row) +
+//    14,336 B float64 summed-area table + 256 B for the largest-value word
+//    = 358,912 B.
+constexpr size_t kNoAllocScratchBytes = 358912;
 
 static __device__ __align__(256) unsigned char g_conv_scratch[kNoAllocScratchBytes];
 

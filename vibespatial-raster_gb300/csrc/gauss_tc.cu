@@ -180,11 +180,6 @@ __device__ __forceinline__ bool g_any(bool p) {
   return r != 0;
 }
 
-__device__ __forceinline__ uint32_t f16x2_bits(__half2 v) {
-  return static_cast<uint32_t>(__half_as_ushort(__low2half(v))) |
-         (static_cast<uint32_t>(__half_as_ushort(__high2half(v))) << 16);
-}
-
 // Four window values (positions 4 grp .. 4 grp + 3) as the 8-byte segments
 // of one K-reversed A row, split z = hi + lo in F16: element klo holds
 // position 4 grp + 3.

@@ -1,4 +1,4 @@
-// tcgen05 building blocks shared by the split-BF16 tensor-core kernels
+// tcgen05 building blocks shared by the split-precision tensor-core kernels
 // (conv_tc.cu: 2-D implicit GEMM; gauss_tc.cu: separable Gaussian line
 // passes): shared-memory matrix descriptors, the BF16 and F16 MMAs with
 // FP32 accumulation, commits, tensor-memory allocation and loads, and the
@@ -111,6 +111,11 @@ __device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, vo
 
 __device__ __forceinline__ uint32_t bf16x2_bits(__nv_bfloat162 v) {
   return static_cast<uint32_t>(__bfloat16_as_ushort(v.x)) | (static_cast<uint32_t>(__bfloat16_as_ushort(v.y)) << 16);
+}
+
+__device__ __forceinline__ uint32_t f16x2_bits(__half2 v) {
+  return static_cast<uint32_t>(__half_as_ushort(__low2half(v))) |
+         (static_cast<uint32_t>(__half_as_ushort(__high2half(v))) << 16);
 }
 
 // 16 consecutive f32 columns of this warp's 32 TMEM lanes, without the

@@ -25,7 +25,8 @@ VSR_U8, VSR_I16, VSR_U16, VSR_I32, VSR_F32, VSR_F64 = 1, 2, 3, 4, 5, 6
 VSR_NODATA_NONE, VSR_NODATA_VALUE, VSR_NODATA_NAN = 0, 1, 2
 VSR_HORN_CENTER_ONLY = 1
 VSR_HORN_SA_NAN_UNMASKED = 2
-VSR_PREC_AUTO, VSR_PREC_FP32, VSR_PREC_SPLIT_BF16 = 0, 1, 2
+VSR_PREC_AUTO, VSR_PREC_FP32, VSR_PREC_SPLIT = 0, 1, 2
+VSR_PREC_SPLIT_BF16 = VSR_PREC_SPLIT  # earlier name of the same code
 VSR_OP_HORN, VSR_OP_BATCH = 1, 2
 VSR_DEVERR_TMA_TIMEOUT, VSR_DEVERR_MMA_TIMEOUT, VSR_DEVERR_QUEUE, VSR_DEVERR_PLAN = 1, 2, 4, 8
 VSR_STAT = {"min": 0, "max": 1, "mean": 2, "std": 3, "range": 4, "variety": 5}

@@ -285,7 +285,10 @@ def raster_terrain(dem: OwnedRasterArray, *, slope: bool = True, aspect: bool = 
 # Normalised focal convolution, Gaussian, focal mean
 # ---------------------------------------------------------------------------
 
-_PRECISION = {"auto": _lib.VSR_PREC_AUTO, "fp32": _lib.VSR_PREC_FP32, "split_bf16": _lib.VSR_PREC_SPLIT_BF16}
+# "split": tcgen05 split-precision GEMMs (BF16 high parts, F16 low parts; see
+# VSR_PREC_SPLIT in vsr.h); "split_bf16" is its earlier name, kept as an alias.
+_PRECISION = {"auto": _lib.VSR_PREC_AUTO, "fp32": _lib.VSR_PREC_FP32, "split": _lib.VSR_PREC_SPLIT,
+              "split_bf16": _lib.VSR_PREC_SPLIT}
 
 
 # ---------------------------------------------------------------------------

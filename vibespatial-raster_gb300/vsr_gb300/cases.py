@@ -63,7 +63,7 @@ def main(argv=None) -> None:
     ap.add_argument("--k", type=int, default=31, help="kernel side (conv, gaussian)")
     ap.add_argument("--sigma", type=float, default=8.0)
     ap.add_argument("--radius", type=int, default=3)
-    ap.add_argument("--precision", default="split_bf16", choices=["auto", "fp32", "split_bf16"])
+    ap.add_argument("--precision", default="split_bf16", choices=["auto", "fp32", "split", "split_bf16"])
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--config", type=int, default=0, help="Horn launch configuration (horn)")
     args = ap.parse_args(argv)
