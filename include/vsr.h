@@ -258,11 +258,17 @@ VSR_API int vsr_convolve_noalloc(const void* src, int dtype, int64_t height, int
  * vsr_gaussian_workspace_size: the FP32 kernels' workspace (a few KB).
  * vsr_gaussian_workspace_bytes: the workspace for a height x width raster of
  * ``dtype`` at ``precision`` (the tensor-core passes need about 8 bytes per
- * pixel); bands of a stack reuse it one after another.
+ * pixel for the row pass's sums).
+ * vsr_gaussian_bands_workspace_bytes: the same for a stack of ``bands``
+ * rasters run as ONE launch per line pass (the row sums of every band held
+ * at once).  vsr_gaussian_bands given less runs the stack in groups of as
+ * many bands as the workspace holds, one launch pair per group.
  */
 VSR_API size_t vsr_gaussian_workspace_size(int kernel_size, int precision);
 VSR_API size_t vsr_gaussian_workspace_bytes(int64_t height, int64_t width, int dtype, double sigma,
                                             int kernel_size, int precision);
+VSR_API size_t vsr_gaussian_bands_workspace_bytes(int bands, int64_t height, int64_t width, int dtype, double sigma,
+                                                  int kernel_size, int precision);
 VSR_API int vsr_gaussian(const void* src, int dtype, int64_t height, int64_t width, int64_t pitch,
                  double sigma, int kernel_size, double nodata, int nodata_kind, void* dst,
                  int out_dtype, int64_t out_pitch, int precision, void* workspace,

@@ -113,3 +113,46 @@ def test_bands_argument_checks(vsr):
                                   _lib.VSR_PREC_FP32, None, 0, None) == _lib.VSR_ERR_INVALID_ARG
     assert lib.vsr_terrain_derivatives_bands(8, _lib.VSR_F32, 2, 100, 10, 10, 10, 1.0, 1.0, 0.0, 0, -9999.0, 8, None,
                                              None, _lib.VSR_F64, 99, 10, None) == _lib.VSR_ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("dtype,shape", [(np.uint16, (150, 200)), (np.uint8, (97, 131))])
+def test_tensor_core_gaussian_bands_one_launch_and_groups(vsr, dtype, shape):
+    """The tensor-core Gaussian over a 3-band stack: one launch pair (room for
+    every band's row sums), groups of two and one band (smaller workspaces),
+    and each band on its own all agree bit for bit; the stack matches the
+    oracle.  The uint8 case has rows that are not 8-byte aligned (the bands
+    are then copied one at a time to an aligned pitch)."""
+    import torch
+
+    from vsr_gb300 import _lib, algebra
+
+    rng = np.random.default_rng(5)
+    hi = 250 if dtype == np.uint8 else 9000
+    stack = rng.integers(1, hi, (3,) + shape).astype(dtype)
+    stack[1, 40:44, 50:55] = 0
+    B, H, W = stack.shape
+    r = vsr.from_numpy(stack, nodata=0)
+    full = algebra.gaussian_bands(r, 6.0, 49, precision="split", out_dtype=np.float32).cpu().numpy()
+    lib = _lib.load()
+    code = _lib.dtype_code(stack.dtype)
+    src = torch.from_numpy(stack).cuda()
+    one = lib.vsr_gaussian_bands_workspace_bytes(1, H, W, code, 6.0, 49, _lib.VSR_PREC_SPLIT)
+    three = lib.vsr_gaussian_bands_workspace_bytes(3, H, W, code, 6.0, 49, _lib.VSR_PREC_SPLIT)
+    assert three > one
+    for nbytes in (one, (one + three) // 2):  # groups of 1, then of 2 + 1
+        ws = torch.empty(nbytes + 256, dtype=torch.uint8, device="cuda")
+        dst = torch.full((B, H, W), -1.0, dtype=torch.float32, device="cuda")
+        p = (ws.data_ptr() + 255) // 256 * 256
+        st = lib.vsr_gaussian_bands(src.data_ptr(), code, B, H * W, H, W, W, 6.0, 49, 0.0, _lib.VSR_NODATA_VALUE,
+                                    dst.data_ptr(), _lib.VSR_F32, H * W, W, _lib.VSR_PREC_SPLIT, p, nbytes, None)
+        _lib.check(st, "vsr_gaussian_bands")
+        np.testing.assert_array_equal(dst.cpu().numpy(), full)
+    w = oracle.gaussian_weights(6.0, 49)
+    for b in range(B):
+        single = algebra.gaussian_bands(vsr.from_numpy(stack[b], nodata=0), 6.0, 49, precision="split",
+                                        out_dtype=np.float32).cpu().numpy()[0]
+        np.testing.assert_array_equal(full[b], single)
+        ref = oracle.convolve_normalized(stack[b], w, 0)
+        m = ref != 0
+        np.testing.assert_array_equal(full[b] == 0, ~m)
+        assert (np.abs(full[b][m] - ref[m]) / np.abs(ref[m])).max() <= 2e-6

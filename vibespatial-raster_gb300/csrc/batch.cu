@@ -15,11 +15,14 @@
 // Work item = (tile, 128 x TH output block).  A CTA claims items with an
 // atomic counter (no waits: an exhausted queue simply ends the CTA), finds
 // the tile by binary search over the per-tile prefix sums, stages
-// (TH + 2*HY) x 136 input values with coalesced loads and clamped
-// coordinates (any pitch or alignment; edge replication for Horn), runs the
-// Horn rows on them, then the separable Gaussian: a row pass into shared
-// memory (numerator and weight sum, validity from coordinates and nodata so
-// out-of-bounds taps are skipped), then the column pass.
+// (TH + 2*HY) x 136 input values one item ahead with cp.async -- 16-byte
+// copies for the 4-column groups inside a 16-byte aligned tile, clamped
+// 4-byte copies elsewhere (any pitch or alignment; edge replication for
+// Horn) -- runs the Horn rows on them, then the separable Gaussian: a row
+// pass into shared memory that forms (numerator, weight sum) pairs with
+// packed f32x2 FMAs (validity from coordinates and nodata, so out-of-bounds
+// taps are skipped), then a column pass down each column with a rolling
+// window of KG row sums in registers.
 namespace vsr {
 namespace {
 
@@ -56,7 +59,7 @@ struct BatchTileDev {
   int64_t items_x;     // blocks across this tile
   int32_t vec;         // outputs 16-byte aligned with pitch % 4 == 0
   float inv8cx, inv8cy;  // 1 / (8 cell), formed in FP64 on the device at plan time
-  int32_t pad_;
+  int32_t vec_in;      // source 16-byte aligned with pitch % 4 == 0 (16-byte staging copies)
 };
 
 struct BatchHeader {  // at the start of the plan
@@ -74,7 +77,8 @@ template <int TH, int THREADS, int KG>
 struct BatchSmem {
   static constexpr int HY = KG / 2 > 0 ? KG / 2 : 1;  // staged halo rows (>= 1 for Horn)
   static constexpr int SR = TH + 2 * HY;              // staged rows
-  static constexpr int kFloats = 2 * SR * kSW + 2 * SR * kTW;  // two staging buffers, row-pass sums
+  static constexpr int RG = TH + 2 * (KG / 2);        // row-pass rows of the Gaussian
+  static constexpr int kFloats = 2 * SR * kSW + 2 * RG * kTW;  // staging x 2, row-pass pairs
 };
 
 
@@ -97,9 +101,8 @@ __global__ void __launch_bounds__(THREADS) batch_terrain_kernel(BatchHeader* __r
   constexpr int HY = L::HY, SR = L::SR;
   static_assert(RB * WARPS == TH && RB % 2 == 0, "rows per warp");
   extern __shared__ __align__(16) float bsm[];
-  float* Sbuf = bsm;                  // 2 x SR x kSW staged values (double buffered)
-  float* Rn = Sbuf + 2 * SR * kSW;    // SR x kTW row-pass numerator
-  float* Rd = Rn + SR * kTW;          // SR x kTW row-pass weight sum
+  float* Sbuf = bsm;                                         // 2 x SR x kSW staged values (double buffered)
+  float2* Rg = reinterpret_cast<float2*>(Sbuf + 2 * SR * kSW);  // RG x kTW (numerator, weight sum) row sums
   __shared__ int64_t sh_first[kBatchSmemTiles];
   __shared__ int64_t sh_item[2];
   __shared__ int sh_tile[2];
@@ -113,7 +116,6 @@ __global__ void __launch_bounds__(THREADS) batch_terrain_kernel(BatchHeader* __r
   float gw[KG > 0 ? KG : 1];
 #pragma unroll
   for (int t = 0; t < KG; ++t) gw[t] = hdr->g[t];
-  const float gs2 = hdr->gsum * hdr->gsum;
   __syncthreads();
 
   // Items are claimed from the atomic counter one ahead of the one being
@@ -158,13 +160,30 @@ __global__ void __launch_bounds__(THREADS) batch_terrain_kernel(BatchHeader* __r
     const int64_t by = local / items_x, bx = local - by * items_x;
     const int64_t x0 = bx * kTW, y0 = by * TH;
     float* S = Sbuf + b * SR * kSW;
-    for (int r = warp; r < SR; r += WARPS) {
-      const int64_t gy = min(max(y0 - HY + r, int64_t(0)), P.height - 1);
-      const float* rowp = T.src + gy * P.in_pitch;
+    if (T.vec_in) {
+      for (int r = warp; r < SR; r += WARPS) {
+        const int64_t gy = min(max(y0 - HY + r, int64_t(0)), P.height - 1);
+        const float* rowp = T.src + gy * P.in_pitch;
+        for (int gq = lane; gq < kSW / 4; gq += 32) {
+          const int64_t gx0 = x0 - 4 + 4 * gq;
+          float* d = S + r * kSW + 4 * gq;
+          if (gx0 >= 0 && gx0 + 3 < P.width) {
+            cp_async16(d, rowp + gx0);
+          } else {
 #pragma unroll
-      for (int c = lane; c < kSW; c += 32) {
-        const int64_t gx = min(max(x0 - 4 + c, int64_t(0)), P.width - 1);
-        cp_async4(S + r * kSW + c, rowp + gx);
+            for (int e = 0; e < 4; ++e) cp_async4(d + e, rowp + min(max(gx0 + e, int64_t(0)), P.width - 1));
+          }
+        }
+      }
+    } else {
+      for (int r = warp; r < SR; r += WARPS) {
+        const int64_t gy = min(max(y0 - HY + r, int64_t(0)), P.height - 1);
+        const float* rowp = T.src + gy * P.in_pitch;
+#pragma unroll
+        for (int c = lane; c < kSW; c += 32) {
+          const int64_t gx = min(max(x0 - 4 + c, int64_t(0)), P.width - 1);
+          cp_async4(S + r * kSW + c, rowp + gx);
+        }
       }
     }
   };
@@ -199,11 +218,6 @@ __global__ void __launch_bounds__(THREADS) batch_terrain_kernel(BatchHeader* __r
     const int64_t H = P.height, W = P.width;
     const float* S = Sbuf + b * SR * kSW;
 
-    // Does the staged block hold nodata?  Clean blocks skip the mask logic.
-    bool any_nd = false;
-    if (P.nd_kind != VSR_NODATA_NONE)
-      for (int i = tid; i < SR * kSW; i += THREADS) any_nd |= is_nd_rt(S[i], P.nd_kind, nd_in);
-    const bool masked = __syncthreads_or(any_nd);
     const bool edge = x0 + kTW > W || y0 + TH > H;
     const MaskRule rule = mask_rule(P);
 
@@ -224,58 +238,63 @@ __global__ void __launch_bounds__(THREADS) batch_terrain_kernel(BatchHeader* __r
     // Gaussian KG x KG (normalised, nodata-aware, out-of-bounds taps skipped).
     if (T.smooth) {
       constexpr int R = KG / 2;
-      const bool exact_den = masked || x0 - R < 0 || y0 - R < 0 || x0 + kTW + R > W || y0 + TH + R > H;
-      // row pass: staged rows (HY-R) .. (HY+TH+R-1), 4 columns per lane
-      for (int r = warp + (HY - R); r < HY + TH + R; r += WARPS) {
+      // row pass: row-sum row rr = staged row rr + HY - R; 4 columns per lane,
+      // (v * valid, valid) pairs summed with packed FMAs (NaN * 0 stays NaN,
+      // as in the reference)
+      const int c0 = 4 * lane;
+      for (int rr = warp; rr < L::RG; rr += WARPS) {
+        const int r = rr + HY - R;
         const int64_t gy = y0 - HY + r;
         const bool row_in = gy >= 0 && gy < H;
-        const int c0 = 4 * lane;
-        float z[4 + KG - 1], vd[4 + KG - 1];
+        const float* sp = S + r * kSW + c0 + 4 - R;
+        float2 zv[4 + KG - 1];
 #pragma unroll
         for (int j = 0; j < 4 + KG - 1; ++j) {
-          const int c = c0 + 4 - R + j;  // staged column
-          const float v = S[r * kSW + c];
-          const int64_t gx = x0 - 4 + c;
+          const float v = sp[j];
+          const int64_t gx = x0 + c0 - R + j;
           const bool ok = row_in && gx >= 0 && gx < W && !is_nd_rt(v, P.nd_kind, nd_in);
-          z[j] = v * (ok ? 1.0f : 0.0f);  // NaN * 0 stays NaN, as in the reference
-          vd[j] = ok ? 1.0f : 0.0f;
+          const float o = ok ? 1.0f : 0.0f;
+          zv[j] = make_float2(v * o, o);
         }
-        float an[4] = {}, ad[4] = {};
+        float2 acc[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) acc[u] = make_float2(0.0f, 0.0f);
 #pragma unroll
         for (int t = 0; t < KG; ++t) {
-          const float w = gw[t];
+          const float2 w2 = make_float2(gw[t], gw[t]);
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            an[u] = fmaf(w, z[u + t], an[u]);
-            ad[u] = fmaf(w, vd[u + t], ad[u]);
-          }
+          for (int u = 0; u < 4; ++u) acc[u] = fma2(w2, zv[u + t], acc[u]);
         }
-        *reinterpret_cast<float4*>(Rn + r * kTW + c0) = make_float4(an[0], an[1], an[2], an[3]);
-        *reinterpret_cast<float4*>(Rd + r * kTW + c0) = make_float4(ad[0], ad[1], ad[2], ad[3]);
+        float4* dst = reinterpret_cast<float4*>(Rg + rr * kTW + c0);
+        dst[0] = make_float4(acc[0].x, acc[0].y, acc[1].x, acc[1].y);
+        dst[1] = make_float4(acc[2].x, acc[2].y, acc[3].x, acc[3].y);
       }
       __syncthreads();
-      // column pass: one column per thread, TH*kTW/THREADS consecutive rows
+      // column pass: column c, RY consecutive output rows, the KG row sums of
+      // the current window held in registers
       constexpr int GROUPS = THREADS / kTW;
       constexpr int RY = TH / GROUPS;
       const int c = tid % kTW;
       const int q0 = (tid / kTW) * RY;
       const int64_t x = x0 + c;
-#pragma unroll 1
-      for (int q = q0; q < q0 + RY; ++q) {
-        const int64_t y = y0 + q;
-        if (y >= H || x >= W) continue;
-        float num = 0.0f, den = 0.0f;
+      float2 win[KG];
 #pragma unroll
-        for (int t = 0; t < KG; ++t) {
-          const int r = q + HY - R + t;
-          const float w = gw[t];
-          num = fmaf(w, Rn[r * kTW + c], num);
-          den = fmaf(w, Rd[r * kTW + c], den);
+      for (int t = 0; t < KG - 1; ++t) win[t] = Rg[(q0 + t) * kTW + c];
+#pragma unroll
+      for (int i = 0; i < RY; ++i) {
+        win[KG - 1] = Rg[(q0 + i + KG - 1) * kTW + c];
+        float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int t = 0; t < KG; ++t) acc = fma2(make_float2(gw[t], gw[t]), win[t], acc);
+#pragma unroll
+        for (int t = 0; t < KG - 1; ++t) win[t] = win[t + 1];
+        const int q = q0 + i;
+        const int64_t y = y0 + q;
+        if (y < H && x < W) {
+          const float cv = S[(q + HY) * kSW + c + 4];
+          const bool centre_ok = !is_nd_rt(cv, P.nd_kind, nd_in);
+          T.smooth[y * T.out_pitch + x] = (centre_ok && acc.y > 0.0f) ? acc.x / acc.y : P.nd_out_f;
         }
-        if (!exact_den) den = gs2;
-        const float cv = S[(q + HY) * kSW + c + 4];
-        const bool centre_ok = !is_nd_rt(cv, P.nd_kind, nd_in);
-        T.smooth[y * T.out_pitch + x] = (centre_ok && den > 0.0f) ? num / den : P.nd_out_f;
       }
     }
     __syncthreads();  // row-pass sums are reused by the next item; buffer b is refilled after the next barrier
@@ -400,7 +419,7 @@ extern "C" int vsr_batch_plan(const vsr_batch_tile* tiles_host, int n_tiles, dou
     d.flags = t.flags;
     d.vec = (!t.slope || (aligned(t.slope, 16) && aligned(t.aspect, 16))) && t.out_pitch % 4 == 0;
     d.inv8cx = d.inv8cy = 0.0f;  // set on the device by prep_batch_cells
-    d.pad_ = 0;
+    d.vec_in = aligned(t.src, 16) && t.pitch % 4 == 0;
     d.items_x = (t.width + kTW - 1) / kTW;
     d.first_item = items;
     items += d.items_x * ((t.height + th - 1) / th);

@@ -32,7 +32,15 @@
 // accumulates in FP32 tensor memory in groups of kernel rows (the
 // accumulation error grows with the number of MMAs chained into one
 // accumulator), the two correction products in one more accumulator; the
-// groups are added in FP32 registers and the sum is scaled back by 1/zs.  The weight sum uses the same split weights, so the
+// groups are added in FP32 registers and the sum is scaled back by 1/zs.
+// The accumulators' rounding grows with their magnitude, so each window
+// row r is also centred on its own mean o_r (when every in-raster tap of the
+// row is valid and finite; else o_r = 0): the A operand holds z - o_r, and
+// -o_r at the row's columns outside the raster, so that every output row m
+// gets back the same sum_ky o[m+ky] * rowsum_ky(w), formed in the epilogue
+// with compensated FP32 arithmetic (error-free products and sums) from the
+// row sums of the split weights.  A smooth raster then leaves only its
+// local noise in the accumulators.  The weight sum uses the same split weights, so the
 // quotient is a consistently weighted mean: on tiles whose window holds no
 // nodata it comes from a summed-area table of w_hi + w_lo (borders only
 // clip the window), otherwise from a 0/1 validity operand times w_hi and
@@ -117,6 +125,8 @@ struct TcPlan {  // shared-memory byte offsets (1024-aligned base) and pipeline 
   uint32_t nanrow;              // 2 x R unsigned __int128 NaN footprints
   uint32_t infrow;              // 2 x R unsigned __int128 +-inf footprints
   uint32_t okrow;               // 2 x R unsigned __int128 validity masks (nodata rules)
+  uint32_t orow;                // 2 x R float row offsets (see the precision note)
+  uint32_t rstab;               // kh float2 (hi, lo) row sums of the split weights
   uint32_t total;
   int nbuf;                     // A buffers (1 or 2)
   int nst;                      // ring stages
@@ -140,7 +150,9 @@ __host__ __device__ inline TcPlan make_plan(const TcGeom& g, bool has_nd, int nb
   p.nanrow = p.ctr + 2 * kM * 8;
   p.infrow = p.nanrow + 2 * static_cast<uint32_t>(g.R) * 16;
   p.okrow = p.infrow + 2 * static_cast<uint32_t>(g.R) * 16;
-  p.total = p.okrow + (has_nd ? 2 * static_cast<uint32_t>(g.R) * 16 : 0u);
+  p.orow = p.okrow + (has_nd ? 2 * static_cast<uint32_t>(g.R) * 16 : 0u);
+  p.rstab = p.orow + ((2 * static_cast<uint32_t>(g.R) * 4 + 15) & ~15u);
+  p.total = p.rstab + static_cast<uint32_t>(g.kh) * 8;
   p.cols = (g.G + 1 + (has_nd ? g.G : 0)) * kTN;  // hh groups | corrections | weight-sum groups
   p.tbuf = 2 * p.cols <= 512 ? 2 : 1;
   return p;
@@ -265,6 +277,15 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
   for (uint32_t i = tid * 16; i < L.ring; i += kThreadsTC * 16)
     *reinterpret_cast<uint4*>(sm + i) = make_uint4(0u, 0u, 0u, 0u);
   for (int i = tid; i < (a.kh + 1) * (a.kw + 1); i += kThreadsTC) sat[i] = a.sat[i];
+  {
+    float2* rs = reinterpret_cast<float2*>(sm + L.rstab);
+    const int S1 = a.kw + 1;
+    for (int ky = tid; ky < a.kh; ky += kThreadsTC) {
+      const double r = (a.sat[(ky + 1) * S1 + a.kw] - a.sat[ky * S1 + a.kw]);
+      const float hi = static_cast<float>(r);
+      rs[ky] = make_float2(hi, static_cast<float>(r - static_cast<double>(hi)));
+    }
+  }
   if (tid == 0) {
     abort_flag = 0;
     for (int i = 0; i < 2; ++i) {
@@ -461,6 +482,23 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
       const double* s_lo = sat + ky_lo * S1;
       const double* s_hi = sat + ky_hi * S1;
       const bool interior = ky_lo == 0 && ky_hi == a.kh && x0 - kw2 >= 0 && x0 + kTN - 1 + (a.kw - 1 - kw2) < a.W;
+      // the row offsets' share of this output row: sum_ky o[m+ky] rowsum_ky,
+      // as a compensated (hi, lo) pair
+      float c_hi = 0.0f, c_lo = 0.0f;
+      {
+        const float* orow = reinterpret_cast<const float*>(sm + L.orow) + slot * g.R + m;
+        const float2* rs = reinterpret_cast<const float2*>(sm + L.rstab);
+        for (int ky = 0; ky < a.kh; ++ky) {
+          const float o = orow[ky];
+          const float2 w = rs[ky];
+          const float p = o * w.x;
+          const float pe = fmaf(o, w.x, -p) + o * w.y;  // the product's rounding error + the lo part
+          const float t = c_hi + p;
+          const float bp = t - c_hi;
+          c_lo += ((c_hi - (t - bp)) + (p - bp)) + pe;
+          c_hi = t;
+        }
+      }
 #pragma unroll 1
       for (int sc = 0; sc < 2; ++sc) {
         const int c0 = chalf * 32 + sc * 16;  // first of this pass's 16 output columns
@@ -504,7 +542,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
             const bool nd = !((cb >> n) & 1u) || !(den[n] > 0.0f);
             ndm |= static_cast<uint32_t>(nd) << n;
             const float inv = (ND == 0 || !den_mma) && interior ? inv_wtot : __frcp_rn(den[n]) * unscale;
-            num[n] = ((fb >> n) & 1u) ? __int_as_float(0x7fc00000) : fmaf(num[n], inv, mu);
+            num[n] = ((fb >> n) & 1u) ? __int_as_float(0x7fc00000) : fmaf((num[n] + c_hi) + c_lo, inv, mu);
           }
           for (uint32_t r = ib & ~ndm; r; r &= r - 1) {  // windows holding +-inf (rare)
             const int n = __ffs(r) - 1;
@@ -574,6 +612,12 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
       uint32_t* nanw = reinterpret_cast<uint32_t*>(sm + L.nanrow) + slot * g.R * 4;
       uint32_t* infw = reinterpret_cast<uint32_t*>(sm + L.infrow) + slot * g.R * 4;
       uint32_t* okw = reinterpret_cast<uint32_t*>(sm + L.okrow) + slot * g.R * 4;
+      float* orow = reinterpret_cast<float*>(sm + L.orow) + slot * g.R;
+      // window columns inside the raster (the same for every row of the tile)
+      int ncols = __popc(colv);
+#pragma unroll
+      for (int o = 16; o; o >>= 1) ncols += __shfl_xor_sync(0xffffffffu, ncols, o);
+      const float inv_ncols = 1.0f / static_cast<float>(ncols > 0 ? ncols : 1);
       unsigned char* ahi = sm + L.a_hi + b * L.a_bytes + o_lane;
       unsigned char* alo = sm + L.a_lo + b * L.a_bytes + o_lane;
       unsigned char* avd = sm + L.a_vd + b * L.a_bytes + o_lane;
@@ -610,6 +654,20 @@ __global__ void __launch_bounds__(kThreadsTC, 1) conv_tc_kernel(const TcArgs a, 
             badm |= static_cast<uint32_t>(inb && !fin) << q;
           }
           if (ND != 0) any_nd |= okm != in;
+          // row offset: the mean of a row whose in-raster taps are all valid
+          // and finite (else 0); columns outside the raster carry -o
+          float o = 0.0f;
+          const bool row_clean = __all_sync(0xffffffffu, okm == in && badm == 0u);  // every lane votes
+          if (yy >= 0 && yy < a.H && row_clean) {  // warp-uniform: one warp per window row
+            float sum = (z[0] + z[1]) + (z[2] + z[3]);
+#pragma unroll
+            for (int sh = 16; sh; sh >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, sh);
+            o = sum * inv_ncols;
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+              z[q] = ((in >> q) & 1u) ? z[q] - o : (kp0 + q < g.KW ? -o : 0.0f);
+          }
+          if (lane == 0) orow[rho] = o;
           if (lane_cols) {
             const __nv_bfloat162 h32 = __floats2bfloat162_rn(z[3], z[2]);
             const __nv_bfloat162 h10 = __floats2bfloat162_rn(z[1], z[0]);

@@ -1257,6 +1257,7 @@ int run_conv_tc(const void* src, int dtype, int bands, int64_t band_stride, int6
                 int64_t out_band_stride, int64_t out_pitch, void* workspace, size_t ws_bytes, cudaStream_t st);
 int gauss_tc_supported(int dtype, int k);  // gauss_tc.cu
 size_t gauss_tc_workspace(int64_t H, int64_t W, int dtype, int k);
+size_t gauss_tc_workspace_bands(int64_t H, int64_t W, int dtype, int k, int bands);
 int run_gauss_tc(const void* src, int dtype, int bands, int64_t band_stride, int64_t H, int64_t W, int64_t pitch,
                  double sigma, int k, double nodata, int nodata_kind, void* dst, int out_dtype,
                  int64_t out_band_stride, int64_t out_pitch, void* workspace, size_t ws_bytes, cudaStream_t st);
@@ -1365,6 +1366,15 @@ extern "C" size_t vsr_gaussian_workspace_bytes(int64_t height, int64_t width, in
   const bool tc = gauss_tc_supported(dtype, k) &&
                   (precision == VSR_PREC_SPLIT || (precision == VSR_PREC_AUTO && k > kMaxSepK));
   return tc ? std::max(gauss_ws(k), gauss_tc_workspace(height, width, dtype, k)) : gauss_ws(k);
+}
+
+extern "C" size_t vsr_gaussian_bands_workspace_bytes(int bands, int64_t height, int64_t width, int dtype,
+                                                     double sigma, int kernel_size, int precision) {
+  if (!(sigma > 0.0) || height < 0 || width < 0 || bands < 1) return 0;
+  const int k = gaussian_size(sigma, kernel_size);
+  const bool tc = gauss_tc_supported(dtype, k) &&
+                  (precision == VSR_PREC_SPLIT || (precision == VSR_PREC_AUTO && k > kMaxSepK));
+  return tc ? std::max(gauss_ws(k), gauss_tc_workspace_bands(height, width, dtype, k, bands)) : gauss_ws(k);
 }
 
 static int gaussian_impl(const void* src, int dtype, int bands, int64_t band_stride, int64_t height, int64_t width,

@@ -63,6 +63,7 @@ namespace vsr {
 
 int gauss_tc_supported(int dtype, int k);
 size_t gauss_tc_workspace(int64_t H, int64_t W, int dtype, int k);
+size_t gauss_tc_workspace_bands(int64_t H, int64_t W, int dtype, int k, int bands);
 int run_gauss_tc(const void* src, int dtype, int bands, int64_t band_stride, int64_t H, int64_t W, int64_t pitch,
                  double sigma, int k, double nodata, int nodata_kind, void* dst, int out_dtype,
                  int64_t out_band_stride, int64_t out_pitch, void* workspace, size_t ws_bytes, cudaStream_t st);
@@ -162,6 +163,10 @@ struct GaussArgs {
   double nd_out;
   const uint16_t* band;  // hi band then lo band
   int k;
+  int bands;             // band-first stack, tiles band-major
+  int64_t src_bstride;   // elements between raster bands (pass 1 src, pass 2 raster)
+  size_t plane_bstride;  // bytes between the chunk planes of consecutive bands
+  int64_t out_bstride;   // elements between output bands (pass 2)
 };
 
 // Named barrier 1 over the converter warps; g_any also ORs a predicate.
@@ -204,8 +209,16 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
   const GaussPlan L = gauss_plan(g, PASS);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t npb = (a.len + kGN - 1) / kGN;
-  const int64_t total = npb * ((a.lines + kGL - 1) / kGL);
+  const int64_t per_band = npb * ((a.lines + kGL - 1) / kGL);
+  const int64_t total = per_band * a.bands;
   const uint32_t s_base = smem_u32(sm);
+  // tile t -> band, first line l0 and first position p0 (band-major order)
+  auto tile_of = [&](int64_t t, int64_t& bd, int64_t& l0, int64_t& p0) {
+    bd = t / per_band;
+    const int64_t rem = t - bd * per_band, lb = rem / npb;
+    l0 = lb * kGL;
+    p0 = (rem - lb * npb) * kGN;
+  };
 
   // ---- set-up: zero the A planes (pass 1: the K padding and the lo rows of
   // the weight-sum operand stay zero for good), load the Toeplitz bands,
@@ -283,9 +296,10 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
           ok = wait_or_abort(&a_empty[b], ((j >> 1) - 1) & 1, &abort_flag, err_word, kDevErrTmaTimeout);
           if (!ok) break;
         }
-        const int64_t lb = t / npb, p0 = (t - lb * npb) * kGN;
-        // chunks p0/8 .. p0/8 + KC - 1 of line block lb, stored in descending order
-        const size_t off = (static_cast<size_t>(lb) * a.np + (a.np - g.KC - p0 / 8)) * kGChunk;
+        int64_t bd, l0, p0;
+        tile_of(t, bd, l0, p0);
+        // chunks p0/8 .. p0/8 + KC - 1 of line block l0/64, stored in descending order
+        const size_t off = bd * a.plane_bstride + (static_cast<size_t>(l0 / kGL) * a.np + (a.np - g.KC - p0 / 8)) * kGChunk;
         mbar_arrive_expect_tx(&a_full[b], 2 * bytes);
         bulk_g2s(sm + 2 * b * L.a_bytes, a.chi + off, bytes, &a_full[b]);
         bulk_g2s(sm + (2 * b + 1) * L.a_bytes, a.clo + off, bytes, &a_full[b]);
@@ -312,13 +326,13 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
     auto raw_slot = [&](int rb, int q, int grp) {
       return sm + L.raw + ((static_cast<uint32_t>(rb) * kGL + cw + kGWarps * q) * g.ngrp + grp) * 8;
     };
-    auto copy_rows = [&](int rb, int64_t l0, int64_t p0) {
+    auto copy_rows = [&](int rb, int64_t bd, int64_t l0, int64_t p0) {
       const int rows = static_cast<int>(a.lines - l0 < kGL ? a.lines - l0 : kGL);  // tile rows inside the raster
       const int64_t rstep = kGWarps * a.pitch * kEsz;
       for (int grp = lane; grp < g.ngrp; grp += 32) {
         const int64_t xb = p0 - g.ra + 4 * grp;
         const int nin = xb < 0 ? 0 : static_cast<int>(a.len - xb > 4 ? 4 : (a.len - xb > 0 ? a.len - xb : 0));
-        const char* gp = static_cast<const char*>(a.src) + ((l0 + cw) * a.pitch + xb) * kEsz;
+        const char* gp = static_cast<const char*>(a.src) + (bd * a.src_bstride + (l0 + cw) * a.pitch + xb) * kEsz;
 #pragma unroll
         for (int q = 0; q < kGLinesPerWarp; ++q, gp += rstep) {
           const bool in = cw + kGWarps * q < rows && nin > 0;
@@ -385,15 +399,16 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
     // bytes, 8-byte pieces spread over the threads (zero-filled outside the
     // raster); read after the copier's wait and a converter barrier.
     constexpr int kCenPieces = kGL * kEsz / 8;  // 8-byte pieces per row
-    auto copy_centres = [&](int cb, int64_t l0, int64_t p0) {
+    auto copy_centres = [&](int cb, int64_t bd, int64_t l0, int64_t p0) {
 #pragma unroll
       for (int k2 = ct; k2 < kGN * kCenPieces; k2 += kGConv) {
         const int row = k2 / kCenPieces, pc = k2 - row * kCenPieces;
         const int64_t y = p0 + row, xb = l0 + pc * (8 / kEsz);
         const int64_t nin = a.lines - xb > 8 / kEsz ? 8 / kEsz : (a.lines - xb > 0 ? a.lines - xb : 0);
         const bool in = y < a.len && nin > 0;
-        const void* gp = in ? static_cast<const void*>(static_cast<const char*>(a.raster) + (y * a.r_pitch + xb) * kEsz)
-                            : a.raster;
+        const void* gp =
+            in ? static_cast<const void*>(static_cast<const char*>(a.raster) + (bd * a.src_bstride + y * a.r_pitch + xb) * kEsz)
+               : a.raster;
         cp_async_zfill<8>(sm + L.raw + (static_cast<uint32_t>(cb) * kGN + row) * 128 + pc * 8, gp,
                           in ? static_cast<uint32_t>(nin * kEsz) : 0u);
       }
@@ -409,7 +424,7 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
     // Tile jj's sums: hi*hi + corrections per TMEM lane (row m: the
     // numerator of line m, or the weight sum of line m - 64) and this
     // warp's 32 positions; cb: its centre buffer (pass 2).
-    auto epilogue = [&](int jj, int64_t l0, int64_t p0, int cb) -> bool {
+    auto epilogue = [&](int jj, int64_t bd, int64_t l0, int64_t p0, int cb) -> bool {
       const int b = jj & 1;
       const int64_t x2 = l0 + i2;
       // one thread waits for the accumulators (and, pass 1, for the previous
@@ -487,7 +502,7 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
           const int cl = ct & 7;
           const int64_t P0 = (l0 + g.ra) / 8;
           if (l0 + 8 * (7 - cl) < ((a.lines + 7) & ~int64_t(7))) {
-            unsigned char* gb = (ct < 8 ? a.chi : a.clo) +
+            unsigned char* gb = (ct < 8 ? a.chi : a.clo) + bd * a.plane_bstride +
                                 (static_cast<size_t>(p0 / kGN) * a.np + (a.np - 1 - P0 - 7 + cl)) * kGChunk;
             bulk_s2g(gb, stg + ((ct >> 3) * 8 + cl) * kGStgChunk, kGChunk);
           }
@@ -515,7 +530,7 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
           const int64_t nrem = (a.len - y0 + 3) / 4;  // rows y0 + 4 q inside the raster
           const int nq = nrem < kGN / 4 ? static_cast<int>(nrem) : kGN / 4;
           if (a.out_dtype == VSR_F64) {
-            double* op = static_cast<double*>(a.dst) + y0 * a.out_pitch + x2;
+            double* op = static_cast<double*>(a.dst) + bd * a.out_bstride + y0 * a.out_pitch + x2;
 #pragma unroll
             for (int q = 0; q < kGN / 4; ++q, op += 4 * a.out_pitch) {
               if (q >= nq) break;
@@ -525,7 +540,7 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
               *op = ok ? static_cast<double>(__fdividef(num, den) * (kGScaleD / kGScaleV)) : a.nd_out;
             }
           } else {
-            float* op = static_cast<float*>(a.dst) + y0 * a.out_pitch + x2;
+            float* op = static_cast<float*>(a.dst) + bd * a.out_bstride + y0 * a.out_pitch + x2;
             const float ndf = static_cast<float>(a.nd_out);
 #pragma unroll
             for (int q = 0; q < kGN / 4; ++q, op += 4 * a.out_pitch) {
@@ -550,26 +565,28 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
     // then tile j-2's epilogue runs.  One cp.async group per iteration.
     int j = 0;
     bool ok = true;
-    int64_t l1 = 0, p1 = 0, l2 = 0, p2 = 0;  // first line / position of tiles j-1 and j-2
+    int64_t b1 = 0, l1 = 0, p1 = 0, b2 = 0, l2 = 0, p2 = 0;  // band / first line / position of tiles j-1, j-2
     if (PASS == 1 && blockIdx.x < total) {
-      const int64_t lb = blockIdx.x / npb;
-      copy_rows(0, lb * kGL, (blockIdx.x - lb * npb) * kGN);
+      int64_t bd, l0, p0;
+      tile_of(blockIdx.x, bd, l0, p0);
+      copy_rows(0, bd, l0, p0);
       cp_async_commit();
     }
     for (int64_t t = blockIdx.x; t < total; t += gridDim.x, ++j) {
-      const int64_t lb = t / npb;
-      const int64_t l0 = lb * kGL, p0 = (t - lb * npb) * kGN;
+      int64_t bd, l0, p0;
+      tile_of(t, bd, l0, p0);
       if (PASS == 1) {
         const int64_t tn = t + gridDim.x;
         if (tn < total) {
-          const int64_t lbn = tn / npb;
-          copy_rows((j + 1) & 1, lbn * kGL, (tn - lbn * npb) * kGN);
+          int64_t bn, ln, pn;
+          tile_of(tn, bn, ln, pn);
+          copy_rows((j + 1) & 1, bn, ln, pn);
         }
       } else {
-        copy_centres(j % kGCenBufs, l0, p0);
+        copy_centres(j % kGCenBufs, bd, l0, p0);
       }
       cp_async_commit();
-      if (j >= 2 && !epilogue(j - 2, l2, p2, (j - 2) % kGCenBufs)) {
+      if (j >= 2 && !epilogue(j - 2, b2, l2, p2, (j - 2) % kGCenBufs)) {
         ok = false;
         break;
       }
@@ -582,8 +599,10 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
         fence_proxy_async_smem();  // generic-proxy operand writes -> visible to the tensor core
         mbar_arrive(&a_full[b]);
       }
+      b2 = b1;
       l2 = l1;
       p2 = p1;
+      b1 = bd;
       l1 = l0;
       p1 = p0;
     }
@@ -591,11 +610,11 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_line_kernel(const GaussArg
     // pass-2 wait count (at most 2 newer groups) right
     if (ok && j >= 2) {
       cp_async_commit();
-      ok = epilogue(j - 2, l2, p2, (j - 2) % kGCenBufs);
+      ok = epilogue(j - 2, b2, l2, p2, (j - 2) % kGCenBufs);
     }
     if (ok && j >= 1) {
       cp_async_commit();
-      epilogue(j - 1, l1, p1, (j - 1) % kGCenBufs);
+      epilogue(j - 1, b1, l1, p1, (j - 1) % kGCenBufs);
     }
     cp_async_wait<0>();
     if (PASS == 1 && ct < 16) bulk_wait_all();  // the output copies are done before the CTA ends
@@ -648,8 +667,8 @@ int launch_gauss_tc(const GaussArgs& p1, const GaussArgs& p2, uint32_t* err, cud
   const size_t s1 = gauss_plan(g, 1).total + 1024, s2 = gauss_plan(g, 2).total + 1024;
   VSR_CUDA_TRY(cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s1)));
   VSR_CUDA_TRY(cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s2)));
-  const int64_t t1 = ((p1.lines + kGL - 1) / kGL) * ((p1.len + kGN - 1) / kGN);
-  const int64_t t2 = ((p2.lines + kGL - 1) / kGL) * ((p2.len + kGN - 1) / kGN);
+  const int64_t t1 = ((p1.lines + kGL - 1) / kGL) * ((p1.len + kGN - 1) / kGN) * p1.bands;
+  const int64_t t2 = ((p2.lines + kGL - 1) / kGL) * ((p2.len + kGN - 1) / kGN) * p2.bands;
   k1<<<static_cast<unsigned>(std::min<int64_t>(t1, sm_count())), kGThreads, s1, st>>>(p1, err);
   VSR_CUDA_TRY(cudaGetLastError());
   k2<<<static_cast<unsigned>(std::min<int64_t>(t2, sm_count())), kGThreads, s2, st>>>(p2, err);
@@ -677,15 +696,20 @@ bool gauss_tc_aligned(const void* band, int64_t pitch, int64_t esz) {
 int64_t gauss_aligned_pitch(int64_t W, int64_t esz) { return (W * esz + 7) / 8 * 8 / esz; }
 }  // namespace
 
-// Workspace: band image | hi chunk plane | lo chunk plane | an aligned copy
-// of one raster band (used when the caller's rows are not 8-byte aligned).
-size_t gauss_tc_workspace(int64_t H, int64_t W, int dtype, int k) {
+// Workspace: band image | an aligned copy of one raster band (used when the
+// caller's rows are not 8-byte aligned) | hi chunk planes of a group of
+// bands | lo chunk planes of the group.  A workspace with room for the
+// planes of every band runs the whole stack in one launch per pass; a
+// smaller one runs the bands in groups (down to one band per launch pair).
+size_t gauss_tc_workspace_bands(int64_t H, int64_t W, int dtype, int k, int bands) {
   const GaussGeom g = gauss_geom(k);
   const int64_t esz = dtype == VSR_U8 ? 1 : 2;
   const size_t band = (static_cast<size_t>(2) * g.NB * 128 + 255) & ~size_t(255);
   const size_t copy = (static_cast<size_t>(H) * gauss_aligned_pitch(W, esz) * esz + 255) & ~size_t(255);
-  return band + 2 * chunk_plane_bytes(H, W, g) + copy;
+  return band + copy + 2 * static_cast<size_t>(bands) * chunk_plane_bytes(H, W, g);
 }
+
+size_t gauss_tc_workspace(int64_t H, int64_t W, int dtype, int k) { return gauss_tc_workspace_bands(H, W, dtype, k, 1); }
 
 int run_gauss_tc(const void* src, int dtype, int bands, int64_t band_stride, int64_t H, int64_t W, int64_t pitch,
                  double sigma, int k, double nodata, int nodata_kind, void* dst, int out_dtype,
@@ -698,12 +722,24 @@ int run_gauss_tc(const void* src, int dtype, int bands, int64_t band_stride, int
   const GaussGeom g = gauss_geom(k);
   const int64_t np = gauss_np(H, g);
   const int64_t nx = (W + kGL - 1) / kGL;
+  const size_t esz = dtype == VSR_U8 ? 1 : 2;
+  const size_t osz = out_dtype == VSR_F64 ? 8 : 4;
+  const int64_t apitch = gauss_aligned_pitch(W, static_cast<int64_t>(esz));
   char* ws = static_cast<char*>(workspace);
   uint16_t* band = reinterpret_cast<uint16_t*>(ws);
-  const size_t off_hi = (static_cast<size_t>(2) * g.NB * 128 + 255) & ~size_t(255);
+  const size_t off_copy = (static_cast<size_t>(2) * g.NB * 128 + 255) & ~size_t(255);
+  const size_t off_planes = off_copy + ((static_cast<size_t>(H) * apitch * esz + 255) & ~size_t(255));
+  void* acopy = ws + off_copy;
   const size_t plane = chunk_plane_bytes(H, W, g);
-  unsigned char* chi = reinterpret_cast<unsigned char*>(ws + off_hi);
-  unsigned char* clo = chi + plane;
+  // bands per launch pair: as many as the workspace holds planes for, when
+  // every band's rows are 8-byte aligned; else one band at a time (each
+  // copied to an aligned pitch when its own rows are not)
+  const bool all_aligned = gauss_tc_aligned(src, pitch, static_cast<int64_t>(esz)) &&
+                           (bands == 1 || (band_stride * static_cast<int64_t>(esz)) % 8 == 0);
+  const int64_t fit = static_cast<int64_t>((ws_bytes - off_planes) / (2 * plane));
+  const int group = all_aligned ? static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(bands, fit))) : 1;
+  unsigned char* chi = reinterpret_cast<unsigned char*>(ws + off_planes);
+  unsigned char* clo = chi + static_cast<size_t>(group) * plane;
   double ndv = 0.0;
   const int kind = resolve_nodata(dtype, nodata, nodata_kind, &ndv);
   uint32_t* err = device_error_word();
@@ -712,29 +748,28 @@ int run_gauss_tc(const void* src, int dtype, int bands, int64_t band_stride, int
   VSR_CUDA_TRY(cudaGetLastError());
   // zero chunks: the padded positions before row 0 (the last ra/8 chunks of
   // each line block) and from round8(H) on (the first chunks); pass 1
-  // writes every other chunk's rows of lines < W
+  // writes every other chunk's rows of lines < W.  The group's planes are
+  // consecutive line blocks of np chunks each.
   const int64_t lead = g.ra / 8, tail = np - (g.ra + ((H + 7) & ~int64_t(7))) / 8;
   for (unsigned char* pl : {chi, clo}) {
-    VSR_CUDA_TRY(cudaMemset2DAsync(pl + (np - lead) * kGChunk, np * kGChunk, 0, lead * kGChunk, nx, st));
-    if (tail > 0) VSR_CUDA_TRY(cudaMemset2DAsync(pl, np * kGChunk, 0, tail * kGChunk, nx, st));
+    VSR_CUDA_TRY(cudaMemset2DAsync(pl + (np - lead) * kGChunk, np * kGChunk, 0, lead * kGChunk, nx * group, st));
+    if (tail > 0) VSR_CUDA_TRY(cudaMemset2DAsync(pl, np * kGChunk, 0, tail * kGChunk, nx * group, st));
   }
-  const size_t esz = dtype == VSR_U8 ? 1 : 2;
-  const size_t osz = out_dtype == VSR_F64 ? 8 : 4;
-  const int64_t apitch = gauss_aligned_pitch(W, static_cast<int64_t>(esz));
-  void* acopy = clo + plane;
-  for (int bi = 0; bi < bands; ++bi) {
-    const void* bsrc = static_cast<const char*>(src) + static_cast<size_t>(bi) * band_stride * esz;
-    void* bdst = static_cast<char*>(dst) + static_cast<size_t>(bi) * out_band_stride * osz;
+  for (int b0 = 0; b0 < bands; b0 += group) {
+    const int nb = std::min(group, bands - b0);
+    const void* bsrc = static_cast<const char*>(src) + static_cast<size_t>(b0) * band_stride * esz;
+    void* bdst = static_cast<char*>(dst) + static_cast<size_t>(b0) * out_band_stride * osz;
     int64_t bp = pitch;
-    if (!gauss_tc_aligned(bsrc, pitch, static_cast<int64_t>(esz))) {
+    if (!gauss_tc_aligned(bsrc, pitch, static_cast<int64_t>(esz))) {  // group == 1 here
       VSR_CUDA_TRY(cudaMemcpy2DAsync(acopy, apitch * esz, bsrc, pitch * esz, W * esz, H, cudaMemcpyDeviceToDevice, st));
       bsrc = acopy;
       bp = apitch;
     }
+    const int64_t sb = nb > 1 ? band_stride : 0, ob = nb > 1 ? out_band_stride : 0;
     GaussArgs p1{bsrc, H, W, bp, chi, clo, np, nullptr, 0, kind, static_cast<int64_t>(ndv),
-                 nullptr, out_dtype, out_pitch, nodata, band, k};
+                 nullptr, out_dtype, out_pitch, nodata, band, k, nb, sb, plane, 0};
     GaussArgs p2{nullptr, W, H, 0, chi, clo, np, bsrc, bp, kind, static_cast<int64_t>(ndv),
-                 bdst, out_dtype, out_pitch, nodata, band, k};
+                 bdst, out_dtype, out_pitch, nodata, band, k, nb, sb, plane, ob};
     int rc = dtype == VSR_U8 ? launch_gauss_tc<VSR_U8>(p1, p2, err, st)
              : dtype == VSR_I16 ? launch_gauss_tc<VSR_I16>(p1, p2, err, st)
                                 : launch_gauss_tc<VSR_U16>(p1, p2, err, st);

@@ -133,6 +133,10 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 __device__ __forceinline__ void cp_async4(void* dst, const void* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
+// 16 bytes, both addresses 16-byte aligned (cached in L2 only).
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
 // BYTES (4 or 8) of which the first ``src_bytes`` are read, the rest zero-filled.
 template <int BYTES>
 __device__ __forceinline__ void cp_async_zfill(void* dst, const void* src, uint32_t src_bytes) {

@@ -94,6 +94,7 @@ SIGNATURES: dict[str, tuple] = {
     ),
     "vsr_gaussian_workspace_size": (_sz, [_int, _int]),
     "vsr_gaussian_workspace_bytes": (_sz, [_i64, _i64, _int, _dbl, _int, _int]),
+    "vsr_gaussian_bands_workspace_bytes": (_sz, [_int, _i64, _i64, _int, _dbl, _int, _int]),
     "vsr_gaussian": (
         _int,
         [_vp, _int, _i64, _i64, _i64, _dbl, _int, _dbl, _int, _vp, _int, _i64, _int, _vp, _sz, _vp],

@@ -462,9 +462,10 @@ def gaussian_bands(raster: OwnedRasterArray, sigma: float, kernel_size: int | No
     dst = out if out is not None else torch.empty((B, H, W), dtype=torch_dtype(odt), device=src.device)
     lib = _lib.load()
     prec = _precision_code(precision)
-    # the tensor-core line passes (split_bf16, and auto on 8/16-bit integer rasters
-    # from k = 35) keep the row pass's sums in about 8 bytes per pixel of workspace
-    nbytes = lib.vsr_gaussian_workspace_bytes(H, W, _lib.dtype_code(dt), float(sigma), k, prec)
+    # the tensor-core line passes (split, and auto on 8/16-bit integer rasters
+    # from k = 35) keep the row pass's sums in about 8 bytes per pixel of
+    # workspace; room for every band's sums runs the stack in one launch per pass
+    nbytes = lib.vsr_gaussian_bands_workspace_bytes(B, H, W, _lib.dtype_code(dt), float(sigma), k, prec)
     ws = _workspace(nbytes, src.device)
     stream = _stream_handle()
     # all bands in one launch (band-first stack, H*W elements apart)
