@@ -1,0 +1,212 @@
+"""libvsr against the reference's OWN GPU kernels, run on the same GPU.
+
+The reference's convolution has no CPU path, and its GPU slope/aspect uses a
+nodata rule (centre pixel only) that its CPU path does not, so these are
+pinned against the reference's kernels themselves: their CUDA C source
+strings (kernels/focal.py) are extracted into the git-ignored oracle/_ref/
+and compiled with this repository's launchers by oracle/make_ref_gpu.py
+(run by build()), then launched with the reference's geometry on float64
+inputs and uint8 nodata masks, as its algebra.py does.
+
+Tolerances: convolution within 1e-5 relative of the reference kernel
+(|out - ref| <= 1e-5 max(|ref|, mean |input|); the split-precision path
+within 2e-6 on the trend raster), NaN and nodata placement exact; slope and
+aspect within 1e-4 degrees (aspect on the circle); hillshade within 1 DN with
+>= 99.5 % exact; focal min / max / range exact, mean and std within 1e-12
+relative, on windows of at most 49 taps and data without NaN (where the
+reference kernel's 49-value variety cap and its NaN handling do not apply).
+Test infrastructure only: nothing in vsr_gb300 imports it.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+LIB = Path(__file__).resolve().parents[1] / "oracle" / "_ref" / "libvsr_refgpu.so"
+
+
+@pytest.fixture(scope="module")
+def ref():
+    if not LIB.exists():
+        pytest.skip("reference-GPU checker not built (oracle/_ref has no extracted kernel sources)")
+    lib = ctypes.CDLL(str(LIB))
+    vp, i, d = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    lib.ref_convolve_normalized.argtypes = [vp, vp, vp, vp, i, i, i, i, d, vp]
+    lib.ref_slope_aspect.argtypes = [vp, vp, vp, vp, i, i, d, d, d, vp]
+    lib.ref_hillshade.argtypes = [vp, vp, vp, i, i, d, d, d, d, d, i, vp]
+    lib.ref_focal_stats.argtypes = [vp, vp, vp, i, i, i, i, i, d, vp]
+    for f in (lib.ref_convolve_normalized, lib.ref_slope_aspect, lib.ref_hillshade, lib.ref_focal_stats):
+        f.restype = i
+    return lib
+
+
+def _dev(a):
+    import torch
+
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _mask(data, nodata):
+    """The reference's device nodata mask (uint8; isnan for a NaN nodata)."""
+    if nodata is None:
+        return None
+    return _dev(oracle.nodata_mask(data, nodata).astype(np.uint8))
+
+
+def _stream():
+    import torch
+
+    return torch.cuda.current_stream().cuda_stream
+
+
+def _ref_convolve(ref, data, w, nodata):
+    import torch
+
+    x = _dev(np.asarray(data, np.float64))
+    out = torch.zeros_like(x)
+    wt = _dev(np.asarray(w, np.float64))
+    m = _mask(data, nodata)
+    H, W = data.shape
+    kh, kw = w.shape
+    nd = float(nodata) if nodata is not None else 0.0
+    assert ref.ref_convolve_normalized(x.data_ptr(), out.data_ptr(), wt.data_ptr(), m.data_ptr() if m is not None else None,
+                                       W, H, kw, kh, nd, _stream()) == 0
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+@pytest.mark.parametrize("shape,k,nodata,precision", [
+    ((90, 140), (5, 5), None, "fp32"), ((77, 130), (3, 7), -9999.0, "fp32"), ((120, 150), (15, 15), None, "fp32"),
+    ((100, 160), (31, 31), -9999.0, "fp32"), ((64, 90), (9, 9), float("nan"), "fp32"),
+    ((150, 208), (31, 31), None, "split"), ((140, 200), (41, 41), None, "split"), ((130, 170), (15, 15), -1.0, "split"),
+])
+def test_convolution_vs_reference_gpu_kernel(vsr, ref, shape, k, nodata, precision):
+    rng = np.random.default_rng(shape[0] + k[0])
+    h, w_ = shape
+    d = (rng.random(shape) + np.arange(h * w_).reshape(shape) * (100.0 / (h * w_))).astype(np.float32)
+    if nodata is not None:
+        d[rng.random(shape) < 0.03] = nodata
+    w = rng.random(k)
+    w /= w.sum()
+    got = vsr.raster_convolve(vsr.from_numpy(d, nodata=nodata), w, precision=precision).to_numpy()
+    want = _ref_convolve(ref, d, w, nodata)
+    np.testing.assert_array_equal(np.isnan(got), np.isnan(want))
+    m = ~np.isnan(want)
+    if nodata is not None and not np.isnan(nodata):
+        np.testing.assert_array_equal(got[m] == nodata, want[m] == nodata)
+    if precision == "split" and nodata is None:
+        err = np.abs(got[m] - want[m]) / np.abs(want[m])
+        assert err.max() <= 2e-6, err.max()
+    else:
+        scale = float(np.nanmean(np.abs(np.where(d == nodata, np.nan, d)))) if nodata is not None else float(np.mean(d))
+        err = np.abs(got[m] - want[m]) / np.maximum(np.abs(want[m]), scale)
+        assert err.max() <= 1e-5, err.max()
+
+
+def test_convolution_nan_poisoning_matches_reference_gpu_kernel(vsr, ref):
+    """NaN data inside a window poisons the reference's sum (NaN * valid);
+    the nodata-centre and empty-window rules give the nodata value."""
+    rng = np.random.default_rng(3)
+    d = rng.normal(10, 2, (60, 80)).astype(np.float32)
+    d[20, 30] = np.nan
+    d[5:9, 60:70] = -5.0
+    w = rng.random((7, 7))
+    w /= w.sum()
+    got = vsr.raster_convolve(vsr.from_numpy(d, nodata=-5.0), w, precision="fp32").to_numpy()
+    want = _ref_convolve(ref, d, w, -5.0)
+    np.testing.assert_array_equal(np.isnan(got), np.isnan(want))
+    m = ~np.isnan(want)
+    np.testing.assert_allclose(got[m], want[m], rtol=1e-5, atol=1e-5)
+
+
+@pytest.mark.parametrize("nodata", [None, -9999.0])
+def test_slope_aspect_center_rule_vs_reference_gpu_kernel(vsr, ref, nodata):
+    import torch
+
+    rng = np.random.default_rng(11)
+    yy, xx = np.mgrid[0:97, 0:150]
+    dem = (800 + 60 * np.sin(yy / 8.0) + 45 * np.cos(xx / 11.0) + rng.normal(0, 1.5, yy.shape)).astype(np.float32)
+    if nodata is not None:
+        dem[rng.random(dem.shape) < 0.02] = nodata
+    aff = (25.0, 0, 0, 0, -25.0, 0)
+    r = vsr.from_numpy(dem, nodata=nodata, affine=aff)
+    s = vsr.raster_slope(r, nodata_mode="center").to_numpy().astype(np.float64)
+    a = vsr.raster_aspect(r, nodata_mode="center").to_numpy().astype(np.float64)
+    x = _dev(dem.astype(np.float64))
+    rs, ra = torch.zeros_like(x), torch.zeros_like(x)
+    m = _mask(dem, nodata)
+    nd = float(nodata) if nodata is not None else 0.0
+    assert ref.ref_slope_aspect(x.data_ptr(), rs.data_ptr(), ra.data_ptr(), m.data_ptr() if m is not None else None,
+                                dem.shape[1], dem.shape[0], 25.0, 25.0, nd, _stream()) == 0
+    torch.cuda.synchronize()
+    rs, ra = rs.cpu().numpy(), ra.cpu().numpy()
+    if nodata is not None:
+        np.testing.assert_array_equal(s == nodata, rs == nodata)
+        keep = rs != nodata
+    else:
+        keep = np.ones(dem.shape, bool)
+    assert np.abs(s[keep] - rs[keep]).max() <= 1e-4
+    dd = np.abs(a[keep] - ra[keep])
+    assert np.minimum(dd, 360.0 - dd).max() <= 1e-4
+
+
+@pytest.mark.parametrize("nodata", [None, -9999.0])
+def test_hillshade_vs_reference_gpu_kernel(vsr, ref, nodata):
+    import math
+
+    import torch
+
+    rng = np.random.default_rng(12)
+    yy, xx = np.mgrid[0:90, 0:131]
+    dem = (300 + 50 * np.sin(yy / 6.0) * np.cos(xx / 9.0) + rng.normal(0, 1.0, yy.shape)).astype(np.float32)
+    if nodata is not None:
+        dem[rng.random(dem.shape) < 0.02] = nodata
+    aff = (10.0, 0, 0, 0, -10.0, 0)
+    h = vsr.raster_hillshade(vsr.from_numpy(dem, nodata=nodata, affine=aff), azimuth=300.0, altitude=40.0).to_numpy()
+    x = _dev(dem.astype(np.float64))
+    out = torch.zeros(dem.shape, dtype=torch.uint8, device="cuda")
+    m = _mask(dem, nodata)
+    assert ref.ref_hillshade(x.data_ptr(), out.data_ptr(), m.data_ptr() if m is not None else None, dem.shape[1],
+                             dem.shape[0], 10.0, 10.0, 1.0, math.radians(90.0 - 40.0), math.radians(300.0), 0,
+                             _stream()) == 0
+    torch.cuda.synchronize()
+    want = out.cpu().numpy()
+    diff = np.abs(h.astype(int) - want.astype(int))
+    assert diff.max() <= 1
+    assert (diff == 0).mean() >= 0.995
+
+
+@pytest.mark.parametrize("stat", ["min", "max", "mean", "std", "range"])
+@pytest.mark.parametrize("dtype,nodata,radius", [(np.float32, -9999.0, (1, 1)), (np.uint16, 0, (3, 2)),
+                                                 (np.float64, None, (2, 3))])
+def test_focal_stats_vs_reference_gpu_kernel(vsr, ref, stat, dtype, nodata, radius):
+    import torch
+
+    from vsr_gb300 import _lib
+
+    rng = np.random.default_rng(13)
+    d = (rng.random((70, 101)) * 500).astype(dtype)
+    if nodata is not None:
+        d[rng.random(d.shape) < 0.05] = nodata
+    ry, rx = radius
+    got = getattr(vsr, f"raster_focal_{stat}")(vsr.from_numpy(d, nodata=nodata), radius).to_numpy()
+    x = _dev(d.astype(np.float64))
+    out = torch.zeros_like(x)
+    m = _mask(d, nodata)
+    nd = float(nodata) if nodata is not None else 0.0
+    assert ref.ref_focal_stats(x.data_ptr(), out.data_ptr(), m.data_ptr() if m is not None else None, d.shape[1],
+                               d.shape[0], rx, ry, _lib.VSR_STAT[stat], nd, _stream()) == 0
+    torch.cuda.synchronize()
+    want = out.cpu().numpy()
+    if stat in ("min", "max", "range"):
+        np.testing.assert_array_equal(got, want)
+    else:
+        np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-12 * 500)
