@@ -17,6 +17,9 @@ It is the small, single-kernel command to run under a profiler:
                 -9999 disc holes (the 16384^2 terrain workload at a chosen
                 size), one launch configuration of the Horn kernel
                 (--config, an index into the tuning table)
+    batch       the first --tiles tiles of the uneven DEM tile batch
+                (slope + aspect + 5 x 5 Gaussian per tile) in one persistent
+                launch, one launch configuration (--config)
 
 Run with ``PYTHONPATH=vibespatial-raster_gb300`` from the repository root.
 """
@@ -57,7 +60,7 @@ def _uint16_stack(bands: int, size: int):
 
 def main(argv=None) -> None:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
-    ap.add_argument("op", choices=["conv", "focal_mean", "gaussian", "horn"])
+    ap.add_argument("op", choices=["conv", "focal_mean", "gaussian", "horn", "batch"])
     ap.add_argument("--size", type=int, default=None, help="raster side (default: 4096 conv, 10980 others)")
     ap.add_argument("--bands", type=int, default=1)
     ap.add_argument("--k", type=int, default=31, help="kernel side (conv, gaussian)")
@@ -65,7 +68,8 @@ def main(argv=None) -> None:
     ap.add_argument("--radius", type=int, default=3)
     ap.add_argument("--precision", default="split_bf16", choices=["auto", "fp32", "split", "split_bf16"])
     ap.add_argument("--reps", type=int, default=5)
-    ap.add_argument("--config", type=int, default=0, help="Horn launch configuration (horn)")
+    ap.add_argument("--config", type=int, default=0, help="launch configuration (horn, batch)")
+    ap.add_argument("--tiles", type=int, default=512, help="tiles of the batch (batch)")
     args = ap.parse_args(argv)
 
     import torch
@@ -96,6 +100,17 @@ def main(argv=None) -> None:
                 torch.empty((1, n, n), dtype=torch.uint8, device=dev))
         ms = _timed(lambda: algebra.horn_fused(r, out=outs), args.reps)
         px = n * n
+    elif args.op == "batch":
+        from vsr_gb300 import _lib, batch
+
+        lib = _lib.load()
+        _lib.check(lib.vsr_tuning_set(_lib.VSR_OP_BATCH, args.config), "vsr_tuning_set")
+        tiles = workloads.tile_batch(device=dev)[: args.tiles]
+        b = batch.TerrainBatch([vsr.from_device(t.data, nodata=t.nodata, affine=t.affine) for t in tiles],
+                               sigma=1.0, kernel_size=5)
+        ms = _timed(b.run, args.reps)
+        n = 0
+        px = sum(int(t.data.numel()) for t in tiles)
     else:
         n = args.size or 10980
         r = vsr.from_device(_uint16_stack(args.bands, n), nodata=0)
