@@ -210,7 +210,7 @@ def autotune_batch(batch: TerrainBatch, *, repeats: int = 3) -> dict:
     return {"config": best, "ms": times}
 
 
-BATCH_CONFIGS = [(32, 256), (64, 256), (16, 128), (32, 128)]  # kBatchConfigs: (rows per block, threads)
+BATCH_CONFIGS = [(32, 128), (48, 128), (64, 256), (16, 128)]  # kBatchConfigs: (rows per block, threads)
 
 __all__ = ["TerrainBatch", "PerTileGraph", "per_tile_launches", "autotune_batch", "BATCH_CONFIGS"]
 
