@@ -1,8 +1,10 @@
-"""Streamed host-to-host terrain pass: row strips with a halo, copies overlapped.
+"""Streamed host-to-host focal passes: row strips with a halo, copies overlapped.
 
 The GB300 counterpart of the reference's out-of-core tiling
 (``dispatch_tiled_halo``, src/vibespatial/raster/tiling.py:468-659, with its
-halo/affine rules at :564-579) for the fused Horn pass.  The DEM stays in
+halo/affine rules at :564-579) for the fused Horn pass (one-row halo) and,
+at the end of this module, for the normalised convolution, the Gaussian and
+the focal statistics (a halo of the window's rows).  The DEM stays in
 host memory (ideally page-locked); it is cut into row strips that carry a
 one-row halo above and below, and each strip goes through
 
@@ -169,3 +171,159 @@ def raster_terrain_host(dem: OwnedRasterArray, *, slope: bool = True, aspect: bo
         res["hillshade"] = from_numpy(o_h, nodata=0 if dem.nodata is not None else None, affine=dem.affine,
                                       crs=dem.crs)
     return res
+
+
+# ---------------------------------------------------------------------------
+# Streamed normalised convolution, Gaussian and focal statistics
+# ---------------------------------------------------------------------------
+
+
+def _focal_host(data: np.ndarray, halo_up: int, halo_down: int, launch, out: np.ndarray, *,
+                strip_rows: int, n_streams: int, ws_bytes: int = 0):
+    """Stream ``data`` (H, W) through ``launch`` in row strips.
+
+    Each strip carries ``halo_up`` / ``halo_down`` real rows around its output
+    rows (fewer at the raster's own edges, where the kernels' out-of-bounds
+    rule applies, as on the whole raster), goes host -> device, through
+    ``launch(d_in, rows, d_out, workspace, workspace_bytes, stream)`` and
+    back into the matching rows of ``out``, round-robin over ``n_streams``
+    CUDA streams so copies and kernels of different strips overlap.
+    """
+    import torch
+
+    H, W = data.shape
+    lib = _lib.load()
+    del lib  # loaded (and checked) before any stream work
+    dev = torch.device("cuda", torch.cuda.current_device())
+    src_t = torch.from_numpy(np.ascontiguousarray(data))
+    dst_t = torch.from_numpy(out)
+    sr = max(1, min(int(strip_rows), H))
+    cap = min(H, sr + halo_up + halo_down)
+    streams = [torch.cuda.Stream(device=dev) for _ in range(n_streams)]
+    bufs = [(torch.empty((cap, W), dtype=src_t.dtype, device=dev), torch.empty((cap, W), dtype=dst_t.dtype, device=dev),
+             torch.empty(max(int(ws_bytes), 256) + 256, dtype=torch.uint8, device=dev)) for _ in range(n_streams)]
+    cur = torch.cuda.current_stream(dev)
+    for s in streams:
+        s.wait_stream(cur)  # buffers were allocated on the current stream
+    for i in range((H + sr - 1) // sr):
+        y0, y1 = i * sr, min(H, (i + 1) * sr)
+        lo, hi = max(0, y0 - halo_up), min(H, y1 + halo_down)
+        s = streams[i % n_streams]
+        d_in, d_out, ws = bufs[i % n_streams]
+        with torch.cuda.stream(s):
+            d_in[: hi - lo].copy_(src_t[lo:hi], non_blocking=True)
+            launch(d_in, hi - lo, d_out, (ws.data_ptr() + 255) // 256 * 256, int(ws_bytes), s.cuda_stream)
+            dst_t[y0:y1].copy_(d_out[y0 - lo:y1 - lo], non_blocking=True)
+    for s in streams:
+        cur.wait_stream(s)
+    cur.synchronize()
+
+
+def _host_plane(raster: OwnedRasterArray):
+    from vsr_gb300.algebra import _WIDEN
+
+    z = np.asarray(raster.to_numpy())
+    if z.ndim == 2:
+        z = z[None]
+    dt = np.dtype(z.dtype)
+    if dt in _WIDEN:
+        z = z.astype(_WIDEN[dt])
+    return z
+
+
+def _stream_result(raster: OwnedRasterArray, outs: np.ndarray) -> OwnedRasterArray:
+    data = outs[0] if np.asarray(raster.data).ndim == 2 else outs
+    return from_numpy(data, nodata=raster.nodata, affine=raster.affine, crs=raster.crs)
+
+
+def raster_convolve_host(raster: OwnedRasterArray, kernel: np.ndarray, *, precision: str = "auto",
+                         out_dtype=np.float64, strip_rows: int = 2048, n_streams: int = 3) -> OwnedRasterArray:
+    """``raster_convolve`` for a host-resident raster with a host-resident result,
+    streamed in row strips with a halo of the kernel's rows (the reference's
+    out-of-core tiling, tiling.py:468-659, halo rule :564-579); for rasters
+    larger than device memory.  Equal to the resident call up to the
+    floating-point order of the per-tile sums."""
+    from vsr_gb300.algebra import _out_code, _precision_code
+
+    w = np.ascontiguousarray(np.asarray(kernel, dtype=np.float64))
+    if w.ndim != 2:
+        raise ValueError(f"kernel must be 2D, got {w.ndim}D")
+    kh, kw = w.shape
+    z = _host_plane(raster)
+    B, H, W = z.shape
+    kind, ndv = nodata_kind(raster)
+    nd = float(raster.nodata) if kind == _lib.VSR_NODATA_VALUE else ndv
+    ocode, odt = _out_code(out_dtype)
+    prec = _precision_code(precision)
+    lib = _lib.load()
+    nbytes = lib.vsr_convolve_workspace_size(kh, kw, prec)
+    wp = w.ctypes.data_as(_lib._c.POINTER(_lib._c.c_double))
+    code = _lib.dtype_code(z.dtype)
+    outs = np.empty((B, H, W), odt)
+
+    def launch(d_in, rows, d_out, ws, ws_bytes, stream):
+        _lib.check(lib.vsr_convolve(d_in.data_ptr(), code, rows, W, W, wp, kh, kw, nd, kind, d_out.data_ptr(), ocode,
+                                    W, prec, ws, ws_bytes, stream), "vsr_convolve")
+
+    for b in range(B):
+        _focal_host(z[b], kh // 2, kh - 1 - kh // 2, launch, outs[b], strip_rows=strip_rows, n_streams=n_streams,
+                    ws_bytes=nbytes)
+    return _stream_result(raster, outs)
+
+
+def raster_gaussian_filter_host(raster: OwnedRasterArray, sigma: float, *, kernel_size: int | None = None,
+                                precision: str = "auto", out_dtype=np.float64, strip_rows: int = 2048,
+                                n_streams: int = 3) -> OwnedRasterArray:
+    """``raster_gaussian_filter`` streamed from and to host memory in row strips
+    with a halo of k // 2 rows (see raster_convolve_host)."""
+    from vsr_gb300.algebra import _out_code, _precision_code, gaussian_kernel_size
+
+    k = gaussian_kernel_size(sigma, kernel_size)
+    z = _host_plane(raster)
+    B, H, W = z.shape
+    kind, ndv = nodata_kind(raster)
+    nd = float(raster.nodata) if kind == _lib.VSR_NODATA_VALUE else ndv
+    ocode, odt = _out_code(out_dtype)
+    prec = _precision_code(precision)
+    lib = _lib.load()
+    code = _lib.dtype_code(z.dtype)
+    rows_max = min(H, int(strip_rows) + 2 * (k // 2))
+    nbytes = lib.vsr_gaussian_workspace_bytes(rows_max, W, code, float(sigma), k, prec)
+    outs = np.empty((B, H, W), odt)
+
+    def launch(d_in, rows, d_out, ws, ws_bytes, stream):
+        _lib.check(lib.vsr_gaussian(d_in.data_ptr(), code, rows, W, W, float(sigma), k, nd, kind, d_out.data_ptr(),
+                                    ocode, W, prec, ws, ws_bytes, stream), "vsr_gaussian")
+
+    for b in range(B):
+        _focal_host(z[b], k // 2, k // 2, launch, outs[b], strip_rows=strip_rows, n_streams=n_streams,
+                    ws_bytes=nbytes)
+    return _stream_result(raster, outs)
+
+
+def raster_focal_host(raster: OwnedRasterArray, stat: str, radius=1, *, out_dtype=np.float64,
+                      strip_rows: int = 2048, n_streams: int = 3) -> OwnedRasterArray:
+    """A focal statistic (``min``, ``max``, ``mean``, ``std``, ``range``,
+    ``variety``; see raster_focal_min etc.) streamed from and to host memory in
+    row strips with a halo of radius_y rows."""
+    from vsr_gb300.algebra import _out_code, _parse_radius
+
+    if stat not in _lib.VSR_STAT:
+        raise ValueError(f"unknown focal statistic {stat!r}; expected one of {sorted(_lib.VSR_STAT)}")
+    ry, rx = _parse_radius(radius)
+    z = _host_plane(raster)
+    B, H, W = z.shape
+    kind, ndv = nodata_kind(raster)
+    nd = float(raster.nodata) if kind == _lib.VSR_NODATA_VALUE else ndv
+    ocode, odt = _out_code(out_dtype)
+    lib = _lib.load()
+    code = _lib.dtype_code(z.dtype)
+    outs = np.empty((B, H, W), odt)
+
+    def launch(d_in, rows, d_out, ws, ws_bytes, stream):
+        _lib.check(lib.vsr_focal_stat(d_in.data_ptr(), code, rows, W, W, _lib.VSR_STAT[stat], ry, rx, nd, kind,
+                                      d_out.data_ptr(), ocode, W, stream), "vsr_focal_stat")
+
+    for b in range(B):
+        _focal_host(z[b], ry, ry, launch, outs[b], strip_rows=strip_rows, n_streams=n_streams)
+    return _stream_result(raster, outs)
