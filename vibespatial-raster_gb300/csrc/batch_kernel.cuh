@@ -28,6 +28,10 @@ namespace bk {
 
 using namespace horn;
 
+__device__ __forceinline__ bool is_nd_rt(float v, int kind, float ndv) {
+  return kind == VSR_NODATA_VALUE ? (v == ndv) : (kind == VSR_NODATA_NAN ? (v != v) : false);
+}
+
 // Horn rows of one batch item for the tile's nodata kind (warp-uniform).
 template <int RB, bool EDGE, bool VEC>
 __device__ __forceinline__ void batch_horn_rows(const float* S, int lane, int r0, int64_t y0, int64_t xs,
@@ -79,32 +83,31 @@ struct BatchSmem {
 };
 
 
+template <int NDK>
+__device__ __forceinline__ bool is_nd_k(float v, float ndv) {
+  if constexpr (NDK == VSR_NODATA_VALUE) return v == ndv;
+  else if constexpr (NDK == VSR_NODATA_NAN) return v != v;
+  else return false;
+}
+
 // The KG x KG Gaussian of one staged item, by each warp for its own RB
 // output rows and its lanes' 4 columns: a horizontal pass per staged row
 // forms (v * valid, valid) pairs with packed FMAs (NaN * 0 stays NaN, as in
-// the reference), a ring of the last KG such row sums in registers gives the
-// vertical pass.  No shared memory beyond the staged block and no barrier:
-// the RB + KG - 1 horizontal passes per RB rows cost less than the occupancy
-// a row-sum buffer would take.  The ring is indexed statically by unrolling
-// one turn of it (KG rows) inside a rolled loop, which keeps the code small
-// (the kernel is instruction-fetch sensitive); the nodata test and the store
-// width are runtime choices for the same reason.
-template <int TH, int THREADS, int KG>
+// the reference), a rolling window of the last KG such row sums in
+// registers gives the vertical pass.  No shared memory beyond the staged
+// block and no barrier: the RB + KG - 1 horizontal passes per RB rows cost
+// less than the occupancy a row-sum buffer would take.
+template <int TH, int THREADS, int KG, int NDK, bool VEC>
 __device__ __forceinline__ void batch_gauss(const float* __restrict__ S, const float (&gw)[KG], int lane, int warp,
-                                            int64_t x0, int64_t y0, int64_t H, int64_t W, int nd_kind, float nd_in,
-                                            float nd_out, bool vec, const BatchTileDev& T) {
+                                            int64_t x0, int64_t y0, int64_t H, int64_t W, float nd_in,
+                                            float nd_out, const BatchTileDev& T) {
   using L = BatchSmem<TH, THREADS, KG>;
   constexpr int WARPS = THREADS / 32;
   constexpr int RB = TH / WARPS;
   constexpr int HY = L::HY;
   constexpr int R = KG / 2;
-  constexpr int NPASS = RB + KG - 1;  // horizontal passes of this warp
   const int c0 = 4 * lane;
   const int q0 = warp * RB;  // first output row of this warp
-  // nodata test without a branch: v == ndv, or v != v for a NaN nodata
-  // (ndv = NaN when the tile has no nodata: nothing compares equal)
-  const float ndv = nd_kind == VSR_NODATA_VALUE ? nd_in : __int_as_float(0x7fc00000);
-  const bool nan_nd = nd_kind == VSR_NODATA_NAN;
   // window columns of this lane inside the tile (bit j: column x0 + c0 - R + j)
   uint32_t colbits = 0;
 #pragma unroll
@@ -119,54 +122,51 @@ __device__ __forceinline__ void batch_gauss(const float* __restrict__ S, const f
   const int nrows = static_cast<int>(H - y0 < TH ? H - y0 : int64_t(TH));  // output rows inside the tile
   const int64_t xs = x0 + c0;
   const int ncols = static_cast<int>(W - xs < 4 ? (W - xs > 0 ? W - xs : 0) : 4);
-  float* const out0 = T.smooth + y0 * T.out_pitch + xs;
-  float2 ring[KG][4];
-#pragma unroll 1
-  for (int i0 = 0; i0 < NPASS; i0 += KG) {
+  float2 win[KG][4];
 #pragma unroll
-    for (int sl = 0; sl < KG; ++sl) {
-      const int i = i0 + sl;  // horizontal pass i lands in ring slot sl (= i mod KG)
-      if (i < NPASS) {
-        const int r = q0 + i + HY - R;  // staged row of this pass
-        const uint32_t bits = (r >= first_in && r < rows_in) ? colbits : 0u;
-        const float* sp = S + r * kSW + c0 + 4 - R;
-        float2 zv[4 + KG - 1];
+  for (int i = 0; i < RB + KG - 1; ++i) {
+    const int r = q0 + i + HY - R;  // staged row of this horizontal pass
+    const uint32_t bits = (r >= first_in && r < rows_in) ? colbits : 0u;
+    const float* sp = S + r * kSW + c0 + 4 - R;
+    float2 zv[4 + KG - 1];
 #pragma unroll
-        for (int j = 0; j < 4 + KG - 1; ++j) {
-          const float v = sp[j];
-          const bool ok = ((bits >> j) & 1u) && !(v == ndv || (nan_nd && v != v));
-          const float o = ok ? 1.0f : 0.0f;
-          zv[j] = make_float2(v * o, o);
+    for (int j = 0; j < 4 + KG - 1; ++j) {
+      const float v = sp[j];
+      const bool ok = ((bits >> j) & 1u) && !is_nd_k<NDK>(v, nd_in);
+      const float o = ok ? 1.0f : 0.0f;
+      zv[j] = make_float2(v * o, o);
+    }
+#pragma unroll
+    for (int t = 0; t < KG - 1; ++t)
+#pragma unroll
+      for (int u = 0; u < 4; ++u) win[t][u] = win[t + 1][u];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) win[KG - 1][u] = make_float2(0.0f, 0.0f);
+#pragma unroll
+    for (int t = 0; t < KG; ++t) {
+      const float2 w2 = make_float2(gw[t], gw[t]);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) win[KG - 1][u] = fma2(w2, zv[u + t], win[KG - 1][u]);
+    }
+    if (i >= KG - 1) {
+      const int q = q0 + i - (KG - 1);  // output row
+      if (q < nrows && ncols > 0) {
+        float o4[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll
+          for (int t = 0; t < KG; ++t) acc = fma2(make_float2(gw[t], gw[t]), win[t][u], acc);
+          const bool centre_ok = !is_nd_k<NDK>(S[(q + HY) * kSW + c0 + 4 + u], nd_in);
+          o4[u] = (centre_ok && acc.y > 0.0f) ? __fdividef(acc.x, acc.y) : nd_out;
         }
+        float* out = T.smooth + (y0 + q) * T.out_pitch + xs;
+        if (VEC && ncols == 4) {
+          __stcs(reinterpret_cast<float4*>(out), make_float4(o4[0], o4[1], o4[2], o4[3]));
+        } else {
 #pragma unroll
-        for (int u = 0; u < 4; ++u) ring[sl][u] = make_float2(0.0f, 0.0f);
-#pragma unroll
-        for (int t = 0; t < KG; ++t) {
-          const float2 w2 = make_float2(gw[t], gw[t]);
-#pragma unroll
-          for (int u = 0; u < 4; ++u) ring[sl][u] = fma2(w2, zv[u + t], ring[sl][u]);
-        }
-        const int q = q0 + i - (KG - 1);  // output row completed by this pass
-        if (i >= KG - 1 && q < nrows && ncols > 0) {
-          float o4[4];
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            float2 acc = make_float2(0.0f, 0.0f);
-#pragma unroll
-            for (int t = 0; t < KG; ++t)  // oldest row of the window first: pass i - KG + 1 + t
-              acc = fma2(make_float2(gw[t], gw[t]), ring[(sl + 1 + t) % KG][u], acc);
-            const float cv = S[(q + HY) * kSW + c0 + 4 + u];
-            const bool centre_ok = !(cv == ndv || (nan_nd && cv != cv));
-            o4[u] = (centre_ok && acc.y > 0.0f) ? __fdividef(acc.x, acc.y) : nd_out;
-          }
-          float* out = out0 + q * T.out_pitch;
-          if (vec && ncols == 4) {
-            __stcs(reinterpret_cast<float4*>(out), make_float4(o4[0], o4[1], o4[2], o4[3]));
-          } else {
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-              if (u < ncols) out[u] = o4[u];
-          }
+          for (int u = 0; u < 4; ++u)
+            if (u < ncols) out[u] = o4[u];
         }
       }
     }
@@ -176,7 +176,7 @@ __device__ __forceinline__ void batch_gauss(const float* __restrict__ S, const f
 constexpr int kBatchSmemTiles = 1024;  // tiles whose prefix sums are searched in shared memory
 
 template <int TH, int THREADS, int KG>
-__global__ void __launch_bounds__(THREADS, 512 / THREADS) batch_terrain_kernel(BatchHeader* __restrict__ hdr,
+__global__ void __launch_bounds__(THREADS) batch_terrain_kernel(BatchHeader* __restrict__ hdr,
                                                                 const BatchTileDev* __restrict__ tiles,
                                                                 uint32_t* err_word) {
   using L = BatchSmem<TH, THREADS, KG>;
@@ -336,8 +336,19 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) batch_terrain_kernel(B
     }
 
     // Gaussian KG x KG (normalised, nodata-aware, out-of-bounds taps skipped).
-    if (T.smooth)
-      batch_gauss<TH, THREADS, KG>(S, gw, lane, warp, x0, y0, H, W, P.nd_kind, nd_in, P.nd_out_f, T.vec_smooth != 0, T);
+    if (T.smooth) {
+      const bool vec = T.vec_smooth != 0;
+      if (P.nd_kind == VSR_NODATA_VALUE) {
+        if (vec) batch_gauss<TH, THREADS, KG, VSR_NODATA_VALUE, true>(S, gw, lane, warp, x0, y0, H, W, nd_in, P.nd_out_f, T);
+        else batch_gauss<TH, THREADS, KG, VSR_NODATA_VALUE, false>(S, gw, lane, warp, x0, y0, H, W, nd_in, P.nd_out_f, T);
+      } else if (P.nd_kind == VSR_NODATA_NAN) {
+        if (vec) batch_gauss<TH, THREADS, KG, VSR_NODATA_NAN, true>(S, gw, lane, warp, x0, y0, H, W, nd_in, P.nd_out_f, T);
+        else batch_gauss<TH, THREADS, KG, VSR_NODATA_NAN, false>(S, gw, lane, warp, x0, y0, H, W, nd_in, P.nd_out_f, T);
+      } else {
+        if (vec) batch_gauss<TH, THREADS, KG, VSR_NODATA_NONE, true>(S, gw, lane, warp, x0, y0, H, W, nd_in, P.nd_out_f, T);
+        else batch_gauss<TH, THREADS, KG, VSR_NODATA_NONE, false>(S, gw, lane, warp, x0, y0, H, W, nd_in, P.nd_out_f, T);
+      }
+    }
     __syncthreads();  // every read of buffer b and of its item slots is done before they are reassigned
   }
   cp_async_wait<0>();  // no copy may land after the CTA leaves
