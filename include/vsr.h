@@ -366,6 +366,33 @@ VSR_API int vsr_batch_plan(const vsr_batch_tile* tiles_host, int n_tiles, double
                    size_t plan_bytes, int64_t* total_items, void* stream);
 VSR_API int vsr_batch_run(void* plan, int gauss_k, void* stream);
 
+/* ---- GeoTIFF decode: chunk assembly on the device -------------------------
+ * The device half of reading a GeoTIFF (reference read_raster, io.py:223, and
+ * its GPU path nvimgcodec_read, nvimgcodec_io.py:221): the host parses the
+ * directory and inflates each chunk (strip or tile) into ``staged`` (device
+ * memory, one chunk after another); this call swaps big-endian samples,
+ * undoes the predictor (1 none, 2 horizontal differencing in the sample's
+ * wrapping integer width, 3 the floating-point byte-plane predictor; 3
+ * rewrites ``staged`` in place) and writes every chunk's in-image pixels to
+ * the band-first output ``dst`` (bands ``band_stride`` elements apart, rows
+ * ``pitch`` elements apart, ``bytes_per_sample`` bytes per element).
+ * ``chunks`` (device memory) describes each chunk: its byte offset in
+ * ``staged``, the pixel rectangle it covers (its stored width and height;
+ * edge tiles may reach past the image) and, for planar-separate files, its
+ * band.  Pixel-interleaved samples (``planar`` = 0, up to 4) go to bands
+ * 0 .. samples_per_pixel-1. */
+typedef struct vsr_tiff_chunk {
+  int64_t offset;         /* byte offset of the chunk in ``staged``            */
+  int32_t x0, y0;         /* image column and row of its first pixel            */
+  int32_t width, height;  /* stored size (tile size, or image width x strip rows) */
+  int32_t band;           /* planar-separate files: the chunk's band            */
+  int32_t pad_;
+} vsr_tiff_chunk;
+VSR_API int vsr_tiff_assemble(uint8_t* staged, const vsr_tiff_chunk* chunks, int n_chunks, int max_chunk_rows,
+                              int bytes_per_sample, int samples_per_pixel, int planar, int predictor, int big_endian,
+                              int64_t height, int64_t width, void* dst, int64_t band_stride, int64_t pitch,
+                              void* stream);
+
 #ifdef __cplusplus
 }
 #endif

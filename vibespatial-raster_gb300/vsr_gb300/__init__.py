@@ -35,10 +35,13 @@ from vsr_gb300.buffers import (  # noqa: F401
     from_device,
     from_numpy,
 )
+from vsr_gb300.io import RasterMetadata, RasterWindow, read_raster, read_raster_metadata  # noqa: F401
 from vsr_gb300.residency import Residency, TransferTrigger  # noqa: F401
 
 __all__ = [
     "OwnedRasterArray",
+    "RasterMetadata",
+    "RasterWindow",
     "RasterDeviceState",
     "RasterDiagnosticEvent",
     "RasterDiagnosticKind",
@@ -63,4 +66,6 @@ __all__ = [
     "raster_terrain_derivatives",
     "raster_tpi",
     "raster_tri",
+    "read_raster",
+    "read_raster_metadata",
 ]

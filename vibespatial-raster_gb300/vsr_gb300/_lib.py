@@ -99,6 +99,10 @@ SIGNATURES: dict[str, tuple] = {
         _int,
         [_vp, _int, _i64, _i64, _i64, _dbl, _int, _dbl, _int, _vp, _int, _i64, _int, _vp, _sz, _vp],
     ),
+    "vsr_tiff_assemble": (
+        _int,
+        [_vp, _vp, _int, _int, _int, _int, _int, _int, _int, _i64, _i64, _vp, _i64, _i64, _vp],
+    ),
     "vsr_batch_plan_size": (_sz, [_int]),
     "vsr_batch_plan": (_int, [_vp, _int, _dbl, _int, _vp, _sz, _c.POINTER(_c.c_int64), _vp]),
     "vsr_batch_run": (_int, [_vp, _int, _vp]),
