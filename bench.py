@@ -493,7 +493,9 @@ def run_vsr(args, ws, rank, local):
         if ws == 1 and not args.no_secondary and H == 16384:
             secondary = {}
             for key, leg in (("C1_slope2048", leg_slope2048), ("C3_conv8192", leg_conv),
-                             ("C4_batch512", leg_batch), ("C5_multiband", leg_multiband)):
+                             ("C4_batch512", leg_batch), ("C5_multiband", leg_multiband),
+                             ("f1_stream_conv", leg_stream), ("f2_derivatives", leg_derivatives),
+                             ("f3_focal_stats", leg_focal_stats), ("f4_decode", leg_decode)):
                 try:
                     secondary[key] = leg(args, dev, local)
                 except Exception as exc:  # a failed leg is reported, the headline still prints
@@ -823,8 +825,192 @@ def leg_derivatives(args, dev, gpu) -> dict:
     }
 
 
+def leg_focal_stats(args, dev, gpu) -> dict:
+    """Focal min / max / std / range / variety (7 x 7) on one 10980^2 uint16 band of the multiband workload."""
+    import torch
+
+    import oracle  # checker and CPU baseline only
+    import vsr_gb300 as vsr
+    from vsr_gb300 import algebra, workloads
+
+    band = workloads.gamma_stack(bands=1, device=dev)
+    _, H, W = band.shape
+    r = vsr.from_device(band, nodata=0)
+    out = torch.empty((1, H, W), dtype=torch.float32, device=dev)
+    hbm, _, src = _peaks()
+    px = H * W
+    per, clocks = {}, None
+    crop = band[0, 2000:2256 + 6, 3000:3256 + 6].cpu().numpy()
+    for stat in ("min", "max", "std", "range", "variety"):
+        fn = lambda: algebra.focal_stat_bands(r, stat, 3, 3, out_dtype=np.float32, out=out)  # noqa: E731
+        for _ in range(3):
+            fn()
+        ms, n, ck = timed_region(fn, 3, gpu, min_seconds=0.3)
+        if stat == "std":
+            clocks = ck
+        got = out[0, 2003:2259, 3003:3259].cpu().numpy().astype(np.float64)
+        t0 = time.perf_counter()
+        ref = oracle.focal_stat(crop, 3, 3, 0, stat)[3:-3, 3:-3]
+        cpu_s = (time.perf_counter() - t0) / ref.size
+        m = np.isfinite(ref)
+        err = np.abs(got[m] - ref[m]) / np.maximum(np.abs(ref[m]), 1.0)
+        per[stat] = {"ms": ms, "gpix_s": px / (ms * 1e-3) / 1e9, "hbm_frac": 6 * px / (ms * 1e-3) / 1e9 / hbm,
+                     "cpu_gpix_s": 1.0 / cpu_s / 1e9, "max_rel_err_vs_fp64": float(err.max()),
+                     "exact": bool(np.array_equal(got[m], ref[m].astype(np.float32).astype(np.float64)))}
+    ms = per["std"]["ms"]
+    return {
+        "workload": f"focal min/max/std/range/variety, 7x7 window, one {H}x{W} uint16 band (gamma(2,800) clipped "
+                    "0-10000, 3% nodata 0), float32 outputs; headline figure: std",
+        "value": px / (ms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms, "gpu_launches": 1, "stats": per,
+        "l2": "241 MB in + 482 MB out per call exceed L2; no flush",
+        "roofline": {"bound": "hbm", "achieved": 6 * px / (ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+                     "frac": 6 * px / (ms * 1e-3) / 1e9 / hbm, "peak_source": src,
+                     "kernel": "focal_stat_kernel<int, std>", "bytes_per_px": 6},
+        "cpu_baseline": {"value": per["std"]["cpu_gpix_s"], "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": "256^2 crop (3-px halo), reference CPU focal statistic (the oracle's "
+                                   "sliding-window restatement), 1 thread, per statistic in 'stats'"},
+        "clocks": clocks,
+    }
+
+
+def leg_decode(args, dev, gpu) -> dict:
+    """GeoTIFF decode onto the GPU: an 8192^2 float32 DEM, 512^2 DEFLATE tiles, floating-point predictor."""
+    import tempfile
+    import zlib as _zlib
+
+    import torch
+
+    import vsr_gb300 as vsr
+    from vsr_gb300 import io, workloads
+
+    dem = workloads.terrain_16k(device=dev, size=8192)
+    host = dem.data.cpu().numpy()
+    H, W = host.shape
+    px = H * W
+    with tempfile.TemporaryDirectory() as tmp:
+        path = Path(tmp) / "dem.tif"
+        io.write_raster(path, vsr.from_numpy(host, nodata=dem.nodata, affine=dem.affine), blockxsize=512,
+                        blockysize=512, level=1)
+        size = path.stat().st_size
+        fn = lambda: io.read_raster(path, residency=vsr.Residency.DEVICE)  # noqa: E731
+        r = fn()
+        ok = bool(torch.equal(r.device_data(), dem.data))
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        sampler = ClockSampler(gpu).start()
+        reps = 5
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        e2e_s = (time.perf_counter() - t0) / reps
+        clocks = sampler.stop()
+        # the device half alone (byte planes undone and tiles assembled): time the
+        # kernel through the C ABI on already inflated chunks
+        with open(path, "rb") as f:
+            t = io._read_ifds(f)[0].tags
+        offs, cnts, geo = io._chunk_layout(t, H, W, 1, False)
+        with open(path, "rb") as f:
+            raw = []
+            for o, c in zip(offs, cnts):
+                f.seek(int(o))
+                raw.append(f.read(int(c)))
+        t0 = time.perf_counter()
+        parts = [_zlib.decompress(b) for b in raw[:16]]
+        cpu_inflate_s = (time.perf_counter() - t0) / (16 * 512 * 512)
+        parts = [_zlib.decompress(b) for b in raw]
+    offsets = np.cumsum([0] + [len(p) for p in parts])
+    staged0 = torch.from_numpy(np.frombuffer(b"".join(parts), np.uint8).copy()).to(dev)
+    table = np.zeros(len(parts), dtype=[("offset", "<i8"), ("x0", "<i4"), ("y0", "<i4"), ("width", "<i4"),
+                                        ("height", "<i4"), ("band", "<i4"), ("pad", "<i4")])
+    for k, g in enumerate(geo):
+        table[k] = (offsets[k], g[0], g[1], g[2], g[3], 0, 0)
+    chunks = torch.from_numpy(table.view(np.uint8).copy()).to(dev)
+    staged = torch.empty_like(staged0)
+    outt = torch.empty((H, W), dtype=torch.int32, device=dev)
+    from vsr_gb300 import _lib
+
+    lib = _lib.load()
+
+    def kern():
+        staged.copy_(staged0)  # predictor 3 works in place
+        _lib.check(lib.vsr_tiff_assemble(staged.data_ptr(), chunks.data_ptr(), len(parts), 512, 4, 1, 0, 3, 0, H, W,
+                                         outt.data_ptr(), H * W, W, torch.cuda.current_stream().cuda_stream),
+                   "vsr_tiff_assemble")
+
+    kern()
+    ms_copy, _, _ = timed_region(lambda: staged.copy_(staged0), 3, gpu, min_seconds=0.2)
+    ms_all, n, _ = timed_region(kern, 3, gpu, min_seconds=0.3)
+    ms_k = max(ms_all - ms_copy, 1e-6)
+    hbm, _, src = _peaks()
+    ach = 12 * px / (ms_k * 1e-3) / 1e9
+    # CPU baseline: the host decode of the same tiles (inflate + byte planes undone + tiles placed), numpy, 1 thread
+    t0 = time.perf_counter()
+    for k in range(4):
+        b = np.frombuffer(parts[k], np.uint8).reshape(512, -1)
+        d = np.cumsum(b, axis=1, dtype=np.uint8)
+        np.ascontiguousarray(d.reshape(512, 4, 512).transpose(0, 2, 1)).view(">f4")
+    cpu_s = (time.perf_counter() - t0) / (4 * 512 * 512) + cpu_inflate_s
+    return {
+        "workload": f"read_raster of a {H}x{W} float32 fBm DEM GeoTIFF ({size / 1e6:.0f} MB), 512x512 DEFLATE tiles, "
+                    "floating-point predictor, into device memory; headline: the device half (byte planes undone, "
+                    "tiles assembled), e2e: the whole call (host directory + inflate on 8 threads + one H2D copy)",
+        "value": px / (ms_k * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms_k, "steps": n, "gpu_launches": 1,
+        "kernel_ms_note": "time of (restore the staged bytes + assemble) minus the restore copy alone",
+        "decoded_equals_source": ok,
+        "e2e": {"value": px / e2e_s / 1e9, "unit": UNIT, "ms_per_call": e2e_s * 1e3, "h2d_bytes_per_call": size},
+        "l2": "268 MB in place + 268 MB out per call exceed L2; no flush",
+        "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                     "peak_source": src, "kernel": "tiff_assemble_kernel (one thread per tile row)",
+                     "bytes_per_px": 12},
+        "cpu_baseline": {"value": 1.0 / cpu_s / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": "16 tiles inflated (zlib) + 4 tiles' byte planes undone (numpy), per-pixel "
+                                   "times summed, 1 thread"},
+        "clocks": clocks,
+    }
+
+
+def leg_stream(args, dev, gpu) -> dict:
+    """Streamed host-to-host 31 x 31 convolution of the 8192^2 raster (row strips with the kernel's halo)."""
+    import torch
+
+    import vsr_gb300 as vsr
+    from vsr_gb300 import stream, workloads
+
+    x = workloads.trend_noise(8192, 8192, device=dev).cpu()
+    host = torch.empty(x.shape, dtype=torch.float32, pin_memory=True)
+    host.copy_(x)
+    r = vsr.from_numpy(host.numpy())
+    w = workloads.random_weights(31, 231)
+    fn = lambda: stream.raster_convolve_host(r, w, precision="split", out_dtype=np.float32, strip_rows=1024)  # noqa: E731
+    fn()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(gpu).start()
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        fn()
+    dt = (time.perf_counter() - t0) / reps
+    clocks = sampler.stop()
+    px = 8192 * 8192
+    link = host_link_peak(dev)
+    link_ms = max(px * 4 / (link["h2d_gbs"] * 1e9), px * 4 / (link["d2h_gbs"] * 1e9)) * 1e3
+    return {
+        "workload": "raster_convolve_host: 8192x8192 f32 U[0,1)+trend from pinned host memory, 31x31 split "
+                    "precision, float32 result in (pageable) host memory, 1024-row strips + 30 halo rows, 3 streams",
+        "value": px / dt / 1e9, "unit": UNIT, "ms_per_step": dt * 1e3, "gpu_launches": 4 * 8,
+        "host_link": link, "link_bound_ms": link_ms, "frac_of_link": link_ms / (dt * 1e3),
+        "roofline": {"bound": "host link", "achieved": 8 * px / dt / 1e9, "peak": link["duplex_gbs"], "unit": "GB/s",
+                     "frac": 8 * px / dt / 1e9 / link["duplex_gbs"], "peak_source": "measured (this run)",
+                     "kernel": "copies + conv_tc_kernel per strip", "bytes_per_px": 8},
+        "cpu_baseline": None,
+        "clocks": clocks,
+    }
+
+
 LEGS = {"slope2048": leg_slope2048, "conv": leg_conv, "batch": leg_batch, "multiband": leg_multiband,
-        "derivatives": leg_derivatives}
+        "derivatives": leg_derivatives, "focal_stats": leg_focal_stats, "decode": leg_decode, "stream": leg_stream}
 
 
 def run_leg(args, ws, rank, local):
@@ -859,7 +1045,8 @@ def main():
                          "split-BF16; batch: 512 uneven tiles, one graph-replayed persistent launch vs per-tile "
                          "launches; multiband: 12 x 10980^2 uint16 focal mean 7x7 + Gaussian 65x65; slope2048: "
                          "slope on a 2048^2 DEM vs the reference CPU fallback; derivatives: TRI + TPI + curvature "
-                         "on the 16384^2 DEM")
+                         "on the 16384^2 DEM; focal_stats: min/max/std/range/variety 7x7 on a 10980^2 uint16 "
+                         "band; decode: GeoTIFF read onto the GPU; stream: host-to-host streamed convolution")
     ap.add_argument("--no-secondary", action="store_true", help="headline only (skip the other configurations)")
     ap.add_argument("--dem-size", type=int, default=16384,
                     help="DEM side (the benchmark workload is 16384; smaller sizes are for profiling)")

@@ -115,3 +115,18 @@ def test_unsupported_codec_and_backend(vsr, tmp_path):
         io.read_raster(p)
     with pytest.raises(NotImplementedError):
         io.read_raster(p, decode_backend="rasterio")
+
+
+@pytest.mark.parametrize("dt", [np.uint8, np.int16, np.uint16, np.int32, np.float32, np.float64])
+@pytest.mark.parametrize("tiled,compress", [(True, "deflate"), (False, "deflate"), (True, None)])
+def test_write_raster_read_raster_round_trip(vsr, tmp_path, dt, tiled, compress):
+    from vsr_gb300 import io
+
+    rng = np.random.default_rng(7)
+    d = _data(dt, (2, 300, 257), rng)
+    r = vsr.from_numpy(d, nodata=None, affine=(3.0, 0.0, 1.0, 0.0, -3.0, 2.0), crs="EPSG:3857")
+    p = tmp_path / "wr.tif"
+    io.write_raster(p, r, compress=compress, tiled=tiled, blockxsize=128, blockysize=64)
+    back = io.read_raster(p)
+    np.testing.assert_array_equal(back.to_numpy().view(f"u{np.dtype(dt).itemsize}"), d.view(f"u{np.dtype(dt).itemsize}"))
+    assert back.affine == r.affine and back.crs == "EPSG:3857"

@@ -44,3 +44,24 @@ def test_rejects_non_tiff(tmp_path):
     p.write_bytes(b"not a tiff at all")
     with pytest.raises(ValueError):
         io.read_raster_metadata(p)
+
+
+def test_write_raster_metadata_and_layout(tmp_path):
+    """write_raster's files parse back to the raster's shape, dtype, affine,
+    CRS and nodata, and their chunks cover the image."""
+    from vsr_gb300 import io
+    from vsr_gb300.buffers import from_numpy
+
+    d = np.arange(2 * 70 * 90, dtype=np.float32).reshape(2, 70, 90)
+    r = from_numpy(d, nodata=-9999.0, affine=(5.0, 0.0, 10.0, 0.0, -5.0, 20.0), crs="EPSG:32632")
+    for tiled in (True, False):
+        p = tmp_path / f"w{tiled}.tif"
+        io.write_raster(p, r, tiled=tiled, blockxsize=32, blockysize=16)
+        m = io.read_raster_metadata(p)
+        assert (m.band_count, m.height, m.width) == (2, 70, 90) and m.dtype == np.float32
+        assert m.affine == (5.0, 0.0, 10.0, 0.0, -5.0, 20.0) and m.crs == "EPSG:32632" and m.nodata == -9999.0
+        with open(p, "rb") as f:
+            t = io._read_ifds(f)[0].tags
+        _, _, geo = io._chunk_layout(t, 70, 90, 2, False)
+        assert len(geo) == (15 if tiled else 5)
+        assert t[259] == (8,) and t[317] == (3,)

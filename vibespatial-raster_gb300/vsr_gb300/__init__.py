@@ -35,7 +35,7 @@ from vsr_gb300.buffers import (  # noqa: F401
     from_device,
     from_numpy,
 )
-from vsr_gb300.io import RasterMetadata, RasterWindow, read_raster, read_raster_metadata  # noqa: F401
+from vsr_gb300.io import RasterMetadata, RasterWindow, read_raster, read_raster_metadata, write_raster  # noqa: F401
 from vsr_gb300.residency import Residency, TransferTrigger  # noqa: F401
 
 __all__ = [
@@ -68,4 +68,5 @@ __all__ = [
     "raster_tri",
     "read_raster",
     "read_raster_metadata",
+    "write_raster",
 ]

@@ -80,12 +80,17 @@ def apply_cached(op: str, h: int, w: int, dtype: str = "float32") -> int | None:
     return int(hit["config"])
 
 
-def autotune_horn(dem, *, repeats: int = 5, outputs=None) -> dict:
+def autotune_horn(dem, *, repeats: int = 8, rounds: int = 3, outputs=None) -> dict:
     """Time every Horn launch configuration on ``dem`` and keep the fastest.
 
-    ``dem`` is an OwnedRasterArray; ``outputs`` optional preallocated output
-    tensors (as for ``algebra.horn_fused(out=...)``).  Returns
-    {"config": i, "shape": (rows, stages, threads), "ms": {i: median ms}}.
+    Each configuration runs ``repeats`` launches back to back between one
+    pair of CUDA events (the steady state a pipeline of launches sees, not
+    an isolated launch); the configurations take turns for ``rounds`` rounds
+    and each keeps its best round, so clock and neighbour drift during the
+    tuning does not decide the choice.  ``dem`` is an OwnedRasterArray;
+    ``outputs`` optional preallocated output tensors (as for
+    ``algebra.horn_fused(out=...)``).  Returns {"config": i, "shape": (rows,
+    stages, threads, CTAs per SM), "ms": {i: best mean ms per launch}}.
     """
     import torch
 
@@ -94,20 +99,21 @@ def autotune_horn(dem, *, repeats: int = 5, outputs=None) -> dict:
     lib = _lib.load()
     n = lib.vsr_tuning_count(_lib.VSR_OP_HORN)
     stream = torch.cuda.current_stream()
-    times = {}
-    for cfg in range(n):
+    times = {cfg: float("inf") for cfg in range(n)}
+    for cfg in range(n):  # warm-up: the first launch of each shape sets its attributes
         _lib.check(lib.vsr_tuning_set(_lib.VSR_OP_HORN, cfg), "vsr_tuning_set")
-        algebra.horn_fused(dem, out=outputs)  # warm-up (first launch sets attributes)
-        samples = []
-        for _ in range(repeats):
+        algebra.horn_fused(dem, out=outputs)
+    for _ in range(rounds):
+        for cfg in range(n):
+            _lib.check(lib.vsr_tuning_set(_lib.VSR_OP_HORN, cfg), "vsr_tuning_set")
+            algebra.horn_fused(dem, out=outputs)
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
-            algebra.horn_fused(dem, out=outputs)
+            for _ in range(repeats):
+                algebra.horn_fused(dem, out=outputs)
             b.record(stream)
             b.synchronize()
-            samples.append(a.elapsed_time(b))
-        samples.sort()
-        times[cfg] = samples[len(samples) // 2]
+            times[cfg] = min(times[cfg], a.elapsed_time(b) / repeats)
     best = min(times, key=times.get)
     _lib.check(lib.vsr_tuning_set(_lib.VSR_OP_HORN, best), "vsr_tuning_set")
     key = cache_key("horn", dem.height, dem.width, str(dem.dtype))

@@ -1,4 +1,4 @@
-"""GeoTIFF reading onto the GPU: ``read_raster`` / ``read_raster_metadata``.
+"""GeoTIFF reading onto the GPU (``read_raster``, ``read_raster_metadata``) and writing (``write_raster``).
 
 Counterparts of the reference's ``read_raster`` (src/vibespatial/raster/io.py:
 223-314), whose GPU path is ``nvimgcodec_read`` (nvimgcodec_io.py:221), and of
@@ -330,3 +330,128 @@ def read_raster(path: str | Path, *, bands: list[int] | None = None, window: Ras
         result.move_to(Residency.HOST, trigger=TransferTrigger.EXPLICIT_RUNTIME_REQUEST,
                        reason="read_raster requested HOST residency")
     return result
+
+
+# ---------------------------------------------------------------------------
+# Write (host-side encoder)
+# ---------------------------------------------------------------------------
+
+
+def _encode_chunk(block: np.ndarray, predictor: int) -> bytes:
+    """One chunk (rows, cols, samples), little-endian, through the predictor."""
+    if predictor == 2:  # differences of consecutive samples, modulo the sample width
+        ut = np.dtype(f"<u{block.dtype.itemsize}")
+        u = np.ascontiguousarray(block).view(ut)
+        d = u.copy()
+        d[:, 1:, :] = u[:, 1:, :] - u[:, :-1, :]
+        return d.tobytes()
+    if predictor == 3:  # byte planes of the big-endian values, differenced along the row
+        rows = block.shape[0]
+        be = np.ascontiguousarray(block.reshape(rows, -1)).astype(block.dtype.newbyteorder(">"))
+        planes = np.frombuffer(be.tobytes(), np.uint8).reshape(rows, -1, block.dtype.itemsize)
+        planes = np.ascontiguousarray(planes.transpose(0, 2, 1)).reshape(rows, -1)
+        d = planes.copy()
+        d[:, 1:] = planes[:, 1:] - planes[:, :-1]
+        return d.tobytes()
+    return np.ascontiguousarray(block).astype(block.dtype.newbyteorder("<")).tobytes()
+
+
+def write_raster(path: str | Path, raster: OwnedRasterArray, *, driver: str = "GTiff", compress: str | None = "deflate",
+                 tiled: bool = True, blockxsize: int = 256, blockysize: int = 256, predictor: int | None = None,
+                 level: int = 6) -> None:
+    """Write a raster as a little-endian GeoTIFF (reference io.py:321-390).
+
+    Tiled (``blockxsize`` x ``blockysize``) or one strip per ``blockysize``
+    rows; DEFLATE or uncompressed; ``predictor`` 1, 2 (integers) or 3
+    (floats), by default 3 for floats and 2 for integers when compressing.
+    BigTIFF when the file would pass 4 GiB.  Affine (ModelPixelScale +
+    ModelTiepoint for north-up affines, else ModelTransformation), CRS
+    (EPSG code) and nodata (GDAL_NODATA) are written.  Encoding runs on the
+    host.
+    """
+    if driver != "GTiff":
+        raise NotImplementedError(f"driver {driver!r}: only GTiff is written")
+    if compress not in (None, "deflate"):
+        raise NotImplementedError(f"compress={compress!r}: only DEFLATE or none")
+    a = np.asarray(raster.to_numpy())
+    if a.ndim == 2:
+        a = a[None]
+    B, H, W = a.shape
+    dt = a.dtype
+    if dt.kind not in "uif" or dt.itemsize not in (1, 2, 4, 8) or (dt.kind == "f" and dt.itemsize < 4):
+        raise NotImplementedError(f"dtype {dt}")
+    if predictor is None:
+        predictor = (3 if dt.kind == "f" else 2) if compress else 1
+    bw, bh = (int(blockxsize), int(blockysize)) if tiled else (W, min(H, int(blockysize)))
+    boxes = [(x0, y0) for y0 in range(0, H, bh) for x0 in range(0, W, bw)]
+
+    def encode(box):
+        x0, y0 = box
+        blk = np.zeros((bh, bw, B), dt)
+        part = a[:, y0:y0 + bh, x0:x0 + bw]
+        blk[: part.shape[1], : part.shape[2], :] = np.moveaxis(part, 0, -1)
+        if not tiled:
+            blk = blk[: part.shape[1]]
+        raw = _encode_chunk(blk, predictor)
+        return zlib.compress(raw, level) if compress else raw
+
+    with ThreadPoolExecutor(max_workers=8) as ex:
+        payload = list(ex.map(encode, boxes))
+    total = sum(len(p) for p in payload)
+    big = total + 65536 > 0xFFFFFFFF
+    tags = [(256, 4, [W]), (257, 4, [H]), (258, 3, [8 * dt.itemsize] * B), (259, 3, [8 if compress else 1]),
+            (262, 3, [1]), (277, 3, [B]), (284, 3, [1]), (339, 3, [{"u": 1, "i": 2, "f": 3}[dt.kind]] * B)]
+    if predictor != 1:
+        tags.append((317, 3, [predictor]))
+    off_t = 16 if big else 4
+    if tiled:
+        tags += [(322, 3, [bw]), (323, 3, [bh]), (324, off_t, [0] * len(payload)), (325, off_t, [len(p) for p in payload])]
+    else:
+        tags += [(273, off_t, [0] * len(payload)), (278, 4, [bh]), (279, off_t, [len(p) for p in payload])]
+    af = tuple(float(v) for v in raster.affine)
+    if af[1] == 0.0 and af[3] == 0.0:
+        tags += [(33550, 12, [af[0], -af[4], 0.0]), (33922, 12, [0.0, 0.0, 0.0, af[2], af[5], 0.0])]
+    else:
+        tags.append((34264, 12, [af[0], af[1], 0.0, af[2], af[3], af[4], 0.0, af[5], 0.0, 0.0, 0.0, 0.0, 0.0,
+                                 0.0, 0.0, 1.0]))
+    crs = getattr(raster, "crs", None)
+    if isinstance(crs, str) and crs.upper().startswith("EPSG:"):
+        code = int(crs.split(":")[1])
+        tags.append((34735, 3, [1, 1, 0, 1, 3072 if code >= 20000 else 2048, 0, 1, code]))
+    if raster.nodata is not None:
+        tags.append((42113, 2, list(repr(float(raster.nodata)).encode() + b"\0")))
+    tags.sort(key=lambda t: t[0])
+    code_of = {2: "B", 3: "H", 4: "I", 12: "d", 16: "Q"}
+    size_of = {2: 1, 3: 2, 4: 4, 12: 8, 16: 8}
+    head, ent, inline = (16, 20, 8) if big else (8, 12, 4)
+    ifd_end = head + (8 if big else 2) + ent * len(tags) + (8 if big else 4)
+    extra = bytearray()
+    where = {}
+    for t, typ, v in tags:
+        n = size_of[typ] * len(v)
+        if n > inline:
+            where[t] = ifd_end + len(extra)
+            extra += bytes(n + (-n) % 8)
+    pos = ifd_end + len(extra)
+    offs = []
+    for p in payload:
+        offs.append(pos)
+        pos += len(p)
+    out = bytearray(b"II" + (struct.pack("<HHHQ", 43, 8, 0, head) if big else struct.pack("<HI", 42, head)))
+    out += struct.pack("<Q" if big else "<H", len(tags))
+    for t, typ, v in tags:
+        if t in (273, 324):
+            v = offs
+        body = struct.pack("<" + code_of[typ] * len(v), *v)
+        if t in where:
+            extra[where[t] - ifd_end: where[t] - ifd_end + len(body)] = body
+            ptr = struct.pack("<Q" if big else "<I", where[t])
+        else:
+            ptr = body + bytes(inline - len(body))
+        out += struct.pack("<HHQ" if big else "<HHI", t, typ, len(v)) + ptr
+    out += bytes(8 if big else 4)
+    with open(path, "wb") as f:
+        f.write(out)
+        f.write(extra)
+        for p in payload:
+            f.write(p)
