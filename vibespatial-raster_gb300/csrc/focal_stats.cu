@@ -79,76 +79,106 @@ __device__ __forceinline__ float max_nan(float a, float b) {
 __device__ __forceinline__ double min_nan(double a, double b) { return (a != a || b != b) ? a + b : fmin(a, b); }
 __device__ __forceinline__ double max_nan(double a, double b) { return (a != a || b != b) ? a + b : fmax(a, b); }
 
-// Element (band b, index idx) as double, with its nodata test.
-__device__ __forceinline__ double fs_load(const FsArgs& a, const char* base, int64_t idx, bool& nodata) {
-  double v;
-  switch (a.dtype) {
-    case VSR_U8: v = __ldg(reinterpret_cast<const uint8_t*>(base) + idx); break;
-    case VSR_I16: v = __ldg(reinterpret_cast<const int16_t*>(base) + idx); break;
-    case VSR_U16: v = __ldg(reinterpret_cast<const uint16_t*>(base) + idx); break;
-    case VSR_I32: v = __ldg(reinterpret_cast<const int32_t*>(base) + idx); break;
-    case VSR_F32: v = __ldg(reinterpret_cast<const float*>(base) + idx); break;
-    default: v = __ldg(reinterpret_cast<const double*>(base) + idx); break;
-  }
-  nodata = a.kind == VSR_NODATA_VALUE ? v == a.ndv : (a.kind == VSR_NODATA_NAN ? v != v : false);
-  return v;
-}
-
-__device__ __forceinline__ int elem_bytes(int dt) {
-  return dt == VSR_U8 ? 1 : (dt == VSR_I16 || dt == VSR_U16) ? 2 : (dt == VSR_F64 ? 8 : 4);
-}
-
 __device__ __forceinline__ void fs_store(const FsArgs& a, char* obase, int64_t idx, double v) {
   if (a.out_dtype == VSR_F64) reinterpret_cast<double*>(obase)[idx] = v;
   else reinterpret_cast<float*>(obase)[idx] = static_cast<float>(v);
 }
 
+// Nodata test in the element type itself (the value is exact there).
+template <typename TIN>
+__device__ __forceinline__ bool is_nd(TIN v, int kind, TIN ndv) {
+  if constexpr (std::is_floating_point<TIN>::value)
+    return kind == VSR_NODATA_VALUE ? v == ndv : (kind == VSR_NODATA_NAN ? v != v : false);
+  else
+    return kind == VSR_NODATA_VALUE && v == ndv;
+}
+
 // Staged value of one tap for statistic S (placeholder for nodata and
 // out-of-bounds taps).
-template <typename T, int S>
-__device__ __forceinline__ T staged(bool inb, bool nodata, double v) {
+template <typename T, int S, typename TIN>
+__device__ __forceinline__ T staged(bool valid, TIN v) {
   if constexpr (std::is_same<T, int32_t>::value) {
-    return (!inb || nodata) ? INT32_MIN : static_cast<int32_t>(v);  // 8/16-bit std
+    return valid ? static_cast<int32_t>(v) : INT32_MIN;  // 8/16-bit std: INT32_MIN is never a value
   } else if constexpr (S == VSR_STAT_MIN) {
-    return (!inb || nodata) ? pos_inf<T>() : static_cast<T>(v);
+    return valid ? static_cast<T>(v) : pos_inf<T>();
   } else if constexpr (S == VSR_STAT_MAX) {
-    return (!inb || nodata) ? -pos_inf<T>() : static_cast<T>(v);
+    return valid ? static_cast<T>(v) : -pos_inf<T>();
   } else {
-    return (!inb || nodata) ? qnan<T>() : static_cast<T>(v);  // NaN data stays NaN = excluded
+    return valid ? static_cast<T>(v) : qnan<T>();  // NaN data stays NaN = excluded
   }
 }
 
-template <typename T, int S>
+template <int S, typename T>
+struct FsLayout {  // shared-memory carve-up of one CTA (byte offsets)
+  static constexpr bool kIntStd = S == VSR_STAT_STD && std::is_same<T, int32_t>::value;
+  static constexpr bool kSep = S == VSR_STAT_MIN || S == VSR_STAT_MAX || S == VSR_STAT_RANGE;
+  __host__ __device__ static size_t staged(int ry, int rx) {
+    return (static_cast<size_t>(kFsTY + 2 * ry) * (kFsTX + 2 * rx) * sizeof(T) + 15) & ~size_t(15);
+  }
+  __host__ __device__ static size_t rows(int ry) {  // row-pass results, (TY + 2 ry) x TX
+    const size_t n = static_cast<size_t>(kFsTY + 2 * ry) * kFsTX;
+    if (kIntStd) return n * (4 + 8 + 4);          // sum, sum of squares, count
+    if (S == VSR_STAT_RANGE) return 2 * n * sizeof(T);
+    if (kSep) return n * sizeof(T);
+    return 0;
+  }
+  __host__ __device__ static size_t total(int ry, int rx) { return staged(ry, rx) + rows(ry) + kFsTY * kFsTX; }
+};
+
+// One CTA = a 64 x 16 output tile of one band.  Staging: the tile's window
+// in the statistic's type with placeholders applied, and the centre
+// pixels' nodata flags.  min / max / range and the 8/16-bit std are
+// separable (a row pass into shared memory, a column pass); the float std
+// (two float64 passes) and variety run over the staged window per pixel.
+template <typename TIN, typename T, int S>
 __global__ void __launch_bounds__(kFsThreads) focal_stat_kernel(const FsArgs a) {
+  using Lay = FsLayout<S, T>;
   extern __shared__ __align__(16) unsigned char fs_smem[];
-  const int SW = kFsTX + 2 * a.rx, SH = kFsTY + 2 * a.ry;
+  const int ry = a.ry, rx = a.rx;
+  const int SW = kFsTX + 2 * rx, SH = kFsTY + 2 * ry;
   T* St = reinterpret_cast<T*>(fs_smem);
+  unsigned char* rows = fs_smem + Lay::staged(ry, rx);
+  unsigned char* ndc = rows + Lay::rows(ry);  // kFsTY x kFsTX centre nodata flags
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int WARPS = kFsThreads / 32;
   const int64_t x0 = static_cast<int64_t>(blockIdx.x) * kFsTX, y0 = static_cast<int64_t>(blockIdx.y) * kFsTY;
-  const char* base = static_cast<const char*>(a.src) + static_cast<int64_t>(blockIdx.z) * a.band_stride * elem_bytes(a.dtype);
+  const TIN* src = static_cast<const TIN*>(a.src) + static_cast<int64_t>(blockIdx.z) * a.band_stride;
   char* obase = static_cast<char*>(a.dst) +
                 static_cast<int64_t>(blockIdx.z) * a.out_band_stride * (a.out_dtype == VSR_F64 ? 8 : 4);
+  const TIN ndv = static_cast<TIN>(a.ndv);  // exact: resolve_nodata checked it fits the element type
+  const int kind = a.kind;
+  // columns of the window inside the raster: [c_lo, c_hi)
+  const int c_lo = x0 - rx >= 0 ? 0 : static_cast<int>(rx - x0);
+  const int64_t chi = a.W - (x0 - rx);
+  const int c_hi = chi < SW ? static_cast<int>(chi) : SW;
 
-  for (int r = warp; r < SH; r += kFsThreads / 32) {
-    const int64_t gy = y0 - a.ry + r;
+  for (int r = warp; r < SH; r += WARPS) {
+    const int64_t gy = y0 - ry + r;
     const bool row_in = gy >= 0 && gy < a.H;
+    const TIN* rowp = src + (row_in ? gy : 0) * a.pitch + (x0 - rx);
+    const bool centre_row = r >= ry && r < ry + kFsTY;
     for (int c = lane; c < SW; c += 32) {
-      const int64_t gx = x0 - a.rx + c;
-      const bool inb = row_in && gx >= 0 && gx < a.W;
-      bool nd = false;
-      double v = 0.0;
-      if (inb) v = fs_load(a, base, gy * a.pitch + gx, nd);
-      St[r * SW + c] = staged<T, S>(inb, nd, v);
+      const bool inb = row_in && c >= c_lo && c < c_hi;
+      const TIN v = inb ? __ldg(rowp + c) : TIN(0);
+      const bool nd = inb && is_nd<TIN>(v, kind, ndv);
+      St[r * SW + c] = staged<T, S, TIN>(inb && !nd, v);
+      if (centre_row && c >= rx && c < rx + kFsTX) ndc[(r - ry) * kFsTX + (c - rx)] = nd;
     }
   }
   __syncthreads();
 
-  if constexpr (S == VSR_STAT_MIN || S == VSR_STAT_MAX || S == VSR_STAT_RANGE) {
-    // Row pass: R0 (min / max / low) and R1 (range high), SH x 64.
-    T* R0 = St + SH * SW;
+  auto out_at = [&](int r, int c, double v) {
+    const int64_t y = y0 + r, x = x0 + c;
+    fs_store(a, obase, y * a.out_pitch + x, ndc[r * kFsTX + c] ? a.nd_out : v);
+  };
+  const int nr = static_cast<int>(a.H - y0 < kFsTY ? a.H - y0 : int64_t(kFsTY));  // output rows inside
+  const int nc = static_cast<int>(a.W - x0 < kFsTX ? a.W - x0 : int64_t(kFsTX));  // output columns inside
+  const int kh = 2 * ry + 1, kw = 2 * rx + 1;
+
+  if constexpr (Lay::kSep) {
+    T* R0 = reinterpret_cast<T*>(rows);
     T* R1 = R0 + SH * kFsTX;
-    const int kw = 2 * a.rx + 1;
-    for (int r = warp; r < SH; r += kFsThreads / 32) {
+    for (int r = warp; r < SH; r += WARPS) {
       const T* row = St + r * SW;
       for (int c = lane; c < kFsTX; c += 32) {
         T m0 = row[c], m1 = row[c];
@@ -163,13 +193,8 @@ __global__ void __launch_bounds__(kFsThreads) focal_stat_kernel(const FsArgs a) 
       }
     }
     __syncthreads();
-    const int kh = 2 * a.ry + 1;
-    for (int r = warp; r < kFsTY; r += kFsThreads / 32) {
-      const int64_t y = y0 + r;
-      if (y >= a.H) break;
-      for (int c = lane; c < kFsTX; c += 32) {
-        const int64_t x = x0 + c;
-        if (x >= a.W) continue;
+    for (int r = warp; r < nr; r += WARPS)
+      for (int c = lane; c < nc; c += 32) {
         T m0 = R0[r * kFsTX + c], m1 = m0;
         if constexpr (S == VSR_STAT_RANGE) m1 = R1[r * kFsTX + c];
         for (int d = 1; d < kh; ++d) {
@@ -181,46 +206,60 @@ __global__ void __launch_bounds__(kFsThreads) focal_stat_kernel(const FsArgs a) 
         if constexpr (S == VSR_STAT_MIN) out = (m0 == pos_inf<T>()) ? a.nd_out : static_cast<double>(m0);
         else if constexpr (S == VSR_STAT_MAX) out = (m0 == -pos_inf<T>()) ? a.nd_out : static_cast<double>(m0);
         else out = (m0 != m0) ? a.nd_out : static_cast<double>(m1) - static_cast<double>(m0);
-        bool nd = false;
-        fs_load(a, base, y * a.pitch + x, nd);
-        fs_store(a, obase, y * a.out_pitch + x, nd ? a.nd_out : out);
+        out_at(r, c, out);
+      }
+  } else if constexpr (Lay::kIntStd) {
+    // exact separable sums: var = (n sum x^2 - (sum x)^2) / n^2
+    int32_t* Rs = reinterpret_cast<int32_t*>(rows);
+    int64_t* Rq = reinterpret_cast<int64_t*>(rows + static_cast<size_t>(SH) * kFsTX * 4);
+    int32_t* Rn = reinterpret_cast<int32_t*>(rows + static_cast<size_t>(SH) * kFsTX * 12);
+    for (int r = warp; r < SH; r += WARPS) {
+      const int32_t* row = reinterpret_cast<const int32_t*>(St) + r * SW;
+      for (int c = lane; c < kFsTX; c += 32) {
+        int32_t sm = 0, n = 0;
+        int64_t q = 0;
+        for (int d = 0; d < kw; ++d) {
+          const int32_t v = row[c + d];
+          const bool ok = v != INT32_MIN;
+          sm += ok ? v : 0;
+          q += ok ? static_cast<int64_t>(v) * v : 0;
+          n += ok;
+        }
+        Rs[r * kFsTX + c] = sm;
+        Rq[r * kFsTX + c] = q;
+        Rn[r * kFsTX + c] = n;
       }
     }
+    __syncthreads();
+    for (int r = warp; r < nr; r += WARPS)
+      for (int c = lane; c < nc; c += 32) {
+        int64_t sm = 0, q = 0;
+        int32_t n = 0;
+        for (int d = 0; d < kh; ++d) {
+          sm += Rs[(r + d) * kFsTX + c];
+          q += Rq[(r + d) * kFsTX + c];
+          n += Rn[(r + d) * kFsTX + c];
+        }
+        out_at(r, c, n ? sqrt(static_cast<double>(static_cast<int64_t>(n) * q - sm * sm)) / n : 0.0);
+      }
   } else {
-    const int kh = 2 * a.ry + 1, kw = 2 * a.rx + 1;
-    for (int r = warp; r < kFsTY; r += kFsThreads / 32) {
-      const int64_t y = y0 + r;
-      if (y >= a.H) break;
-      for (int c = lane; c < kFsTX; c += 32) {
-        const int64_t x = x0 + c;
-        if (x >= a.W) continue;
+    for (int r = warp; r < nr; r += WARPS)
+      for (int c = lane; c < nc; c += 32) {
         const T* win = St + r * SW + c;
         double out;
-        if constexpr (S == VSR_STAT_STD && std::is_same<T, int32_t>::value) {
-          int64_t s = 0, q = 0;
-          int n = 0;
-          for (int dy = 0; dy < kh; ++dy)
-            for (int dx = 0; dx < kw; ++dx) {
-              const int32_t v = win[dy * SW + dx];
-              if (v == INT32_MIN) continue;
-              s += v;
-              q += static_cast<int64_t>(v) * v;
-              ++n;
-            }
-          out = n ? sqrt(static_cast<double>(static_cast<int64_t>(n) * q - s * s)) / n : 0.0;
-        } else if constexpr (S == VSR_STAT_STD) {
-          double s = 0.0;
+        if constexpr (S == VSR_STAT_STD) {
+          double sm = 0.0;
           int n = 0;
           for (int dy = 0; dy < kh; ++dy)
             for (int dx = 0; dx < kw; ++dx) {
               const double v = win[dy * SW + dx];
               if (v != v) continue;
-              s += v;
+              sm += v;
               ++n;
             }
           double m2 = 0.0;
           if (n) {
-            const double mean = s / n;
+            const double mean = sm / n;
             for (int dy = 0; dy < kh; ++dy)
               for (int dx = 0; dx < kw; ++dx) {
                 const double v = win[dy * SW + dx];
@@ -230,7 +269,7 @@ __global__ void __launch_bounds__(kFsThreads) focal_stat_kernel(const FsArgs a) 
               }
           }
           out = n ? sqrt(m2 / n) : 0.0;
-        } else {  // variety
+        } else {  // variety: taps with no equal earlier tap
           int cnt = 0;
           for (int iy = 0; iy < kh; ++iy)
             for (int ix = 0; ix < kw; ++ix) {
@@ -246,27 +285,15 @@ __global__ void __launch_bounds__(kFsThreads) focal_stat_kernel(const FsArgs a) 
             }
           out = cnt;
         }
-        bool nd = false;
-        fs_load(a, base, y * a.pitch + x, nd);
-        fs_store(a, obase, y * a.out_pitch + x, nd ? a.nd_out : out);
+        out_at(r, c, out);
       }
-    }
   }
 }
 
-template <typename T, int S>
-size_t fs_smem(int ry, int rx) {
-  const size_t SW = kFsTX + 2 * rx, SH = kFsTY + 2 * ry;
-  size_t b = SW * SH * sizeof(T);
-  if (S == VSR_STAT_MIN || S == VSR_STAT_MAX) b += SH * kFsTX * sizeof(T);
-  if (S == VSR_STAT_RANGE) b += 2 * SH * kFsTX * sizeof(T);
-  return b;
-}
-
-template <typename T, int S>
+template <typename TIN, typename T, int S>
 int fs_launch(const FsArgs& a, int bands, cudaStream_t st) {
-  const size_t smem = fs_smem<T, S>(a.ry, a.rx);
-  auto kern = focal_stat_kernel<T, S>;
+  const size_t smem = FsLayout<S, T>::total(a.ry, a.rx);
+  auto kern = focal_stat_kernel<TIN, T, S>;
   VSR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   const dim3 grid(static_cast<unsigned>((a.W + kFsTX - 1) / kFsTX), static_cast<unsigned>((a.H + kFsTY - 1) / kFsTY),
                   static_cast<unsigned>(bands));
@@ -275,14 +302,29 @@ int fs_launch(const FsArgs& a, int bands, cudaStream_t st) {
   return VSR_OK;
 }
 
+// T: the statistic's type -- float for 8/16-bit and float32 rasters (exact),
+// double for int32 / float64, int32 for the 8/16-bit std (exact int sums).
 template <int S>
 int fs_dispatch(const FsArgs& a, int bands, cudaStream_t st) {
-  const bool wide = a.dtype == VSR_I32 || a.dtype == VSR_F64;
   if constexpr (S == VSR_STAT_STD) {
-    if (a.dtype == VSR_U8 || a.dtype == VSR_I16 || a.dtype == VSR_U16) return fs_launch<int32_t, S>(a, bands, st);
-    return fs_launch<double, S>(a, bands, st);
+    switch (a.dtype) {
+      case VSR_U8: return fs_launch<uint8_t, int32_t, S>(a, bands, st);
+      case VSR_I16: return fs_launch<int16_t, int32_t, S>(a, bands, st);
+      case VSR_U16: return fs_launch<uint16_t, int32_t, S>(a, bands, st);
+      case VSR_I32: return fs_launch<int32_t, double, S>(a, bands, st);
+      case VSR_F32: return fs_launch<float, double, S>(a, bands, st);
+      default: return fs_launch<double, double, S>(a, bands, st);
+    }
+  } else {
+    switch (a.dtype) {
+      case VSR_U8: return fs_launch<uint8_t, float, S>(a, bands, st);
+      case VSR_I16: return fs_launch<int16_t, float, S>(a, bands, st);
+      case VSR_U16: return fs_launch<uint16_t, float, S>(a, bands, st);
+      case VSR_I32: return fs_launch<int32_t, double, S>(a, bands, st);
+      case VSR_F32: return fs_launch<float, float, S>(a, bands, st);
+      default: return fs_launch<double, double, S>(a, bands, st);
+    }
   }
-  return wide ? fs_launch<double, S>(a, bands, st) : fs_launch<float, S>(a, bands, st);
 }
 
 }  // namespace
