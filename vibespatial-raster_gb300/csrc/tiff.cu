@@ -4,7 +4,7 @@
 //
 // The host parses the TIFF directory and inflates the chunks (strips or
 // tiles) into one staging buffer; vsr_tiff_assemble then, on the GPU, for
-// every chunk row (one thread per row, or per row and sample):
+// every chunk row (one warp per row, its lanes over the row's values):
 //   * swaps the bytes of big-endian files,
 //   * undoes the predictor: 2 = horizontal differencing, a running sum per
 //     sample in the sample's own wrapping integer type; 3 = the floating-point
@@ -39,11 +39,26 @@ struct TiffArgs {
   int max_rows;                // largest chunk height
 };
 
-// One thread per (chunk, chunk row); grid-stride over all of them.
+// Inclusive prefix sum of one value per lane over the warp (wrapping in
+// the value's width is the caller's mask).
+__device__ __forceinline__ uint64_t warp_scan(uint64_t v, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint64_t n = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += n;
+  }
+  return v;
+}
+
+// One warp per (chunk, chunk row), grid-stride over all of them.  Lanes
+// take consecutive values, so loads and stores are coalesced; the running
+// sums of the predictors are warp scans carried from one 32-value step to
+// the next.
 __global__ void tiff_assemble_kernel(const TiffArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
   const int64_t total = static_cast<int64_t>(a.n_chunks) * a.max_rows;
-  for (int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; t < total;
-       t += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+  for (int64_t t = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; t < total; t += warps) {
     const int ci = static_cast<int>(t / a.max_rows), r = static_cast<int>(t - static_cast<int64_t>(ci) * a.max_rows);
     const vsr_tiff_chunk c = a.chunks[ci];
     if (r >= c.height) continue;
@@ -53,35 +68,58 @@ __global__ void tiff_assemble_kernel(const TiffArgs a) {
     uint8_t* row = a.staged + c.offset + static_cast<int64_t>(r) * row_vals * a.esz;
     const int64_t ncols = c.x0 + static_cast<int64_t>(c.width) <= a.W ? c.width : a.W - c.x0;
     if (a.predictor == 3) {
-      // byte planes: undo the byte-wise differencing over the whole row, then
-      // value i's bytes are plane b at i (b = 0 most significant)
+      // byte planes: undo the byte-wise differencing over the whole row (a
+      // wrapping byte scan, 32 lanes x 4 bytes per step), then value i's
+      // bytes are plane b at i (b = 0 most significant)
       const int64_t nb = row_vals * a.esz;
-      for (int64_t i = 1; i < nb; ++i) row[i] = static_cast<uint8_t>(row[i] + row[i - 1]);
+      uint32_t carry = 0;
+      for (int64_t b0 = 0; b0 < nb; b0 += 128) {
+        const int64_t i0 = b0 + 4 * lane;
+        uint32_t v0 = 0, v1 = 0, v2 = 0, v3 = 0;
+        if (i0 + 0 < nb) v0 = row[i0 + 0];
+        if (i0 + 1 < nb) v1 = row[i0 + 1];
+        if (i0 + 2 < nb) v2 = row[i0 + 2];
+        if (i0 + 3 < nb) v3 = row[i0 + 3];
+        v1 += v0;
+        v2 += v1;
+        v3 += v2;
+        const uint32_t incl = static_cast<uint32_t>(warp_scan(v3, lane));
+        const uint32_t excl = incl - v3 + carry;
+        if (i0 + 0 < nb) row[i0 + 0] = static_cast<uint8_t>(v0 + excl);
+        if (i0 + 1 < nb) row[i0 + 1] = static_cast<uint8_t>(v1 + excl);
+        if (i0 + 2 < nb) row[i0 + 2] = static_cast<uint8_t>(v2 + excl);
+        if (i0 + 3 < nb) row[i0 + 3] = static_cast<uint8_t>(v3 + excl);
+        carry += __shfl_sync(0xffffffffu, incl, 31);
+      }
+      __syncwarp();
       if (y >= a.H) continue;
-      for (int64_t x = 0; x < ncols; ++x)
-        for (int s = 0; s < ns; ++s) {
-          const int64_t i = x * ns + s;
-          uint64_t v = 0;
-          for (int b = 0; b < a.esz; ++b) v = (v << 8) | row[b * row_vals + i];
-          const int band = a.planar ? c.band : s;
-          store_elem(a.dst + (band * a.band_stride + y * a.pitch + c.x0 + x) * a.esz, a.esz, v);
-        }
-      continue;
-    }
-    if (y >= a.H) continue;
-    uint64_t acc[4] = {0, 0, 0, 0};
-    const uint64_t mask = a.esz == 8 ? ~0ull : ((1ull << (8 * a.esz)) - 1ull);
-    for (int64_t x = 0; x < ncols; ++x)
-      for (int s = 0; s < ns; ++s) {
-        uint64_t v = load_elem(row + (x * ns + s) * a.esz, a.esz, a.swap);
-        if (a.predictor == 2) {  // wrapping sum in the sample's own width
-          const int k = s < 4 ? s : 3;
-          acc[k] = (acc[k] + v) & mask;
-          v = acc[k];
-        }
+      for (int64_t i = lane; i < ncols * ns; i += 32) {
+        uint64_t v = 0;
+        for (int b = 0; b < a.esz; ++b) v = (v << 8) | row[b * row_vals + i];
+        const int64_t x = i / ns;
+        const int s = static_cast<int>(i - x * ns);
         const int band = a.planar ? c.band : s;
         store_elem(a.dst + (band * a.band_stride + y * a.pitch + c.x0 + x) * a.esz, a.esz, v);
       }
+      continue;
+    }
+    if (y >= a.H) continue;
+    const uint64_t mask = a.esz == 8 ? ~0ull : ((1ull << (8 * a.esz)) - 1ull);
+    for (int s = 0; s < ns; ++s) {
+      const int band = a.planar ? c.band : s;
+      uint8_t* orow = a.dst + (band * a.band_stride + y * a.pitch + c.x0) * a.esz;
+      uint64_t carry = 0;
+      for (int64_t x0 = 0; x0 < ncols; x0 += 32) {
+        const int64_t x = x0 + lane;
+        uint64_t v = x < ncols ? load_elem(row + (x * ns + s) * a.esz, a.esz, a.swap) : 0;
+        if (a.predictor == 2) {  // running sum of the differences, wrapping in the sample's width
+          const uint64_t incl = warp_scan(v, lane);
+          v = (incl + carry) & mask;
+          carry += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        if (x < ncols) store_elem(orow + x * a.esz, a.esz, v);
+      }
+    }
   }
 }
 
@@ -106,9 +144,9 @@ extern "C" int vsr_tiff_assemble(uint8_t* staged, const vsr_tiff_chunk* chunks, 
     return fail(VSR_ERR_INVALID_ARG, "output pitch / band stride too small");
   TiffArgs a{staged, chunks, n_chunks, bytes_per_sample, samples_per_pixel, planar ? 1 : 0, predictor,
              big_endian ? 1 : 0, height, width, static_cast<uint8_t*>(dst), band_stride, pitch, max_chunk_rows};
-  const int64_t total = static_cast<int64_t>(n_chunks) * max_chunk_rows;
-  const int threads = 128;
-  const int64_t blocks = std::min<int64_t>((total + threads - 1) / threads, static_cast<int64_t>(sm_count()) * 16);
+  const int64_t total = static_cast<int64_t>(n_chunks) * max_chunk_rows;  // one warp each
+  const int threads = 256;
+  const int64_t blocks = std::min<int64_t>((total * 32 + threads - 1) / threads, static_cast<int64_t>(sm_count()) * 16);
   tiff_assemble_kernel<<<static_cast<unsigned>(blocks > 0 ? blocks : 1), threads, 0, static_cast<cudaStream_t>(stream)>>>(a);
   VSR_CUDA_TRY(cudaGetLastError());
   return VSR_OK;

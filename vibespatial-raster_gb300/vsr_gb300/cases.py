@@ -18,8 +18,8 @@ It is the small, single-kernel command to run under a profiler:
                 size), one launch configuration of the Horn kernel
                 (--config, an index into the tuning table)
     batch       the first --tiles tiles of the uneven DEM tile batch
-                (slope + aspect + 5 x 5 Gaussian per tile) in one persistent
-                launch, one launch configuration (--config)
+                (slope + aspect + 5 x 5 Gaussian per tile, or --part) in one
+                persistent launch, one launch configuration (--config)
 
 Run with ``PYTHONPATH=vibespatial-raster_gb300`` from the repository root.
 """
@@ -70,6 +70,9 @@ def main(argv=None) -> None:
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--config", type=int, default=0, help="launch configuration (horn, batch)")
     ap.add_argument("--tiles", type=int, default=512, help="tiles of the batch (batch)")
+    ap.add_argument("--part", default="all", choices=["all", "horn", "gauss"],
+                    help="batch: slope + aspect + Gaussian, or one of the two alone")
+    ap.add_argument("--no-nodata", action="store_true", help="batch: tiles without a nodata value")
     args = ap.parse_args(argv)
 
     import torch
@@ -106,8 +109,9 @@ def main(argv=None) -> None:
         lib = _lib.load()
         _lib.check(lib.vsr_tuning_set(_lib.VSR_OP_BATCH, args.config), "vsr_tuning_set")
         tiles = workloads.tile_batch(device=dev)[: args.tiles]
-        b = batch.TerrainBatch([vsr.from_device(t.data, nodata=t.nodata, affine=t.affine) for t in tiles],
-                               sigma=1.0, kernel_size=5)
+        rs = [vsr.from_device(t.data, nodata=None if args.no_nodata else t.nodata, affine=t.affine) for t in tiles]
+        b = batch.TerrainBatch(rs, terrain=args.part != "gauss", sigma=None if args.part == "horn" else 1.0,
+                               kernel_size=5)
         ms = _timed(b.run, args.reps)
         n = 0
         px = sum(int(t.data.numel()) for t in tiles)

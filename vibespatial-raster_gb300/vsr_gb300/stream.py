@@ -219,6 +219,16 @@ def _focal_host(data: np.ndarray, halo_up: int, halo_down: int, launch, out: np.
     cur.synchronize()
 
 
+def _pinned_empty(shape, dtype) -> np.ndarray:
+    """A page-locked host array (the device -> host copies of the strips then
+    run asynchronously instead of blocking the host between strips)."""
+    import torch
+
+    from vsr_gb300.buffers import torch_dtype
+
+    return torch.empty(shape, dtype=torch_dtype(np.dtype(dtype)), pin_memory=True).numpy()
+
+
 def _host_plane(raster: OwnedRasterArray):
     from vsr_gb300.algebra import _WIDEN
 
@@ -259,7 +269,7 @@ def raster_convolve_host(raster: OwnedRasterArray, kernel: np.ndarray, *, precis
     nbytes = lib.vsr_convolve_workspace_size(kh, kw, prec)
     wp = w.ctypes.data_as(_lib._c.POINTER(_lib._c.c_double))
     code = _lib.dtype_code(z.dtype)
-    outs = np.empty((B, H, W), odt)
+    outs = _pinned_empty((B, H, W), odt)
 
     def launch(d_in, rows, d_out, ws, ws_bytes, stream):
         _lib.check(lib.vsr_convolve(d_in.data_ptr(), code, rows, W, W, wp, kh, kw, nd, kind, d_out.data_ptr(), ocode,
@@ -289,7 +299,7 @@ def raster_gaussian_filter_host(raster: OwnedRasterArray, sigma: float, *, kerne
     code = _lib.dtype_code(z.dtype)
     rows_max = min(H, int(strip_rows) + 2 * (k // 2))
     nbytes = lib.vsr_gaussian_workspace_bytes(rows_max, W, code, float(sigma), k, prec)
-    outs = np.empty((B, H, W), odt)
+    outs = _pinned_empty((B, H, W), odt)
 
     def launch(d_in, rows, d_out, ws, ws_bytes, stream):
         _lib.check(lib.vsr_gaussian(d_in.data_ptr(), code, rows, W, W, float(sigma), k, nd, kind, d_out.data_ptr(),
@@ -318,7 +328,7 @@ def raster_focal_host(raster: OwnedRasterArray, stat: str, radius=1, *, out_dtyp
     ocode, odt = _out_code(out_dtype)
     lib = _lib.load()
     code = _lib.dtype_code(z.dtype)
-    outs = np.empty((B, H, W), odt)
+    outs = _pinned_empty((B, H, W), odt)
 
     def launch(d_in, rows, d_out, ws, ws_bytes, stream):
         _lib.check(lib.vsr_focal_stat(d_in.data_ptr(), code, rows, W, W, _lib.VSR_STAT[stat], ry, rx, nd, kind,
