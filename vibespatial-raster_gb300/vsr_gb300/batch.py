@@ -70,9 +70,13 @@ class TerrainBatch:
                 raise ValueError("batched tiles must be single-band float32 rasters")
             t = r.device_data().contiguous()
             H, W = t.shape
-            slope = torch.empty((H, W), dtype=torch.float32, device=t.device) if terrain else None
-            aspect = torch.empty((H, W), dtype=torch.float32, device=t.device) if terrain else None
-            smooth = torch.empty((H, W), dtype=torch.float32, device=t.device) if self.k else None
+            # outputs with rows padded to 16 bytes (views of W columns): the kernel
+            # then stores 4 pixels per 128-bit store whatever the tile's width
+            Wp = (W + 3) // 4 * 4
+            mk = lambda: torch.empty((H, Wp), dtype=torch.float32, device=t.device)[:, :W]  # noqa: E731
+            slope = mk() if terrain else None
+            aspect = mk() if terrain else None
+            smooth = mk() if self.k else None
             self.inputs.append(t)
             self.outputs.append((slope, aspect, smooth))
             kind, ndv = nodata_kind(r)
@@ -81,7 +85,7 @@ class TerrainBatch:
                                slope.data_ptr() if slope is not None else None,
                                aspect.data_ptr() if aspect is not None else None,
                                smooth.data_ptr() if smooth is not None else None,
-                               W, cx, cy, ndv if kind != _lib.VSR_NODATA_NONE else 0.0, kind,
+                               Wp, cx, cy, ndv if kind != _lib.VSR_NODATA_NONE else 0.0, kind,
                                _lib.VSR_HORN_SA_NAN_UNMASKED)
         self._tiles = arr
         nbytes = self.lib.vsr_batch_plan_size(len(rasters))
