@@ -146,16 +146,19 @@ def test_focal_mean_known_answer(vsr):
     assert any(e.detail.startswith("gpu_focal_mean") for e in vsr.raster_focal_mean(vsr.from_numpy(d), 1).diagnostics)
 
 
-@pytest.mark.parametrize("dtype,r", [(np.uint16, 3), (np.int16, 7), (np.uint8, 5), (np.uint16, 1)])
+@pytest.mark.parametrize("dtype,r", [(np.uint16, 3), (np.int16, 7), (np.uint8, 5), (np.uint16, 1),
+                                     (np.int16, 4), (np.uint8, 2), (np.uint16, 4), (np.int16, 2)])
 def test_focal_mean_integer_sliding_window(vsr, dtype, r):
-    """Square windows on 8/16-bit rasters (the packed sliding-window kernel):
-    several 256-row strips and 128-column blocks with ragged edges, odd row
-    pitch (no paired loads) and even pitch, exact float64 means and correctly
-    rounded float32 means."""
+    """Square windows on 8/16-bit rasters (the packed sliding-window kernels):
+    several 256-row strips and column blocks with ragged edges; an odd row
+    pitch (the shared-memory kernel, no paired loads) and pitches that are
+    multiples of 4 (the register-resident kernel for radii up to 4: 120-column
+    warp strips, 480-column blocks, ragged at 964 = 2 x 480 + 4); exact
+    float64 means and correctly rounded float32 means."""
     rng = np.random.default_rng(r)
     lo, hi = {np.uint16: (0, 65535), np.int16: (-32767, 32767), np.uint8: (0, 254)}[dtype]
     nd = {np.uint16: 0, np.int16: -32768, np.uint8: 255}[dtype]
-    for shape in [(600, 389), (300, 1024)]:
+    for shape in [(600, 389), (300, 1024), (530, 964), (9, 4)]:
         d = rng.integers(lo, hi, shape, endpoint=True).astype(dtype)
         d[rng.random(shape) < 0.03] = nd
         d[:20, :30] = nd  # a window with no valid value

@@ -1183,8 +1183,196 @@ __global__ void __launch_bounds__(kSlTW) box_slide_int(const BoxArgs a) {
   }
 }
 
+// ------------------------------------------------------- box_warp_int --
+// The same focal mean (8/16-bit integers, square (2R+1)^2 window) for
+// R <= 4 when rows are aligned to 4 elements, held in registers.
+//
+// One warp owns a 128-column strip, 4 columns per lane; lanes 0 and 31 only
+// supply their columns to their neighbours, so a warp writes the 120 columns
+// of lanes 1-30 and consecutive warps overlap by 8 columns.  Per input row
+// each lane loads its 4 elements (one vector load, prefetched 2R+1 rows
+// ahead), packs them as value | count words (the packing of box_slide_int),
+// takes R words from each neighbour by shuffles and forms its 4 horizontal
+// window sums by sliding; the vertical window slides over a register ring of
+// the last 2R+1 horizontal sums, with the row loop unrolled by 2R+1 so that
+// every ring index is a compile-time constant.  The float32 quotient is the
+// same correctly rounded division as box_slide_int's.
+constexpr int kBwLanes = 30;            // output lanes per warp
+constexpr int kBwCols = 4 * kBwLanes;   // output columns per warp
+constexpr int kBwWarps = 4;             // warps per block, side by side
+constexpr int kBwStrip = 256;           // output rows per warp
+
+template <typename T>
+struct Vec4Of {  // 4 elements in one load
+  using type = uint2;
+};
+template <>
+struct Vec4Of<uint8_t> {
+  using type = uint32_t;
+};
+
+template <int R, typename T, bool VOUT>
+__global__ void __launch_bounds__(32 * kBwWarps) box_warp_int(const BoxArgs a) {
+  static_assert(R >= 1 && R <= 4, "the neighbour exchange covers radii up to 4");
+  using Pk = SlidePack<R>;
+  using V4 = typename Vec4Of<T>::type;
+  constexpr int P = 2 * R + 1;
+  constexpr int OFF = std::is_signed<T>::value ? 32768 : 0;
+  constexpr uint32_t kOne = 1u << Pk::kShift, kLow = kOne - 1u;
+  static_assert(Pk::kShift <= 23, "value sums must stay below 2^23 for the float conversion");
+  __shared__ float2 tab[Pk::kTaps + 1];  // (RN(1/n), n)
+  for (int i = threadIdx.x; i <= Pk::kTaps; i += blockDim.x)
+    tab[i] = make_float2(i ? __frcp_rn(static_cast<float>(i)) : 0.0f, static_cast<float>(i));
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int64_t xw = (static_cast<int64_t>(blockIdx.x) * kBwWarps + (threadIdx.x >> 5)) * kBwCols;
+  if (xw >= a.W) return;  // the whole warp: no block-wide barrier follows
+  const int64_t xs = xw - 4 + 4 * lane;  // this lane's first column (a multiple of 4)
+  const int64_t ys = static_cast<int64_t>(blockIdx.y) * kBwStrip;
+  const T* src = static_cast<const T*>(band_src(a.src, a.dtype, a.band_stride));
+  void* dst = band_dst(a.dst, a.out_dtype, a.out_band_stride);
+  const int nout = static_cast<int>(a.H - ys < kBwStrip ? a.H - ys : kBwStrip);
+  const int nin = nout + 2 * R;  // input rows ys - R .. ys + nout + R - 1
+  const bool has_nd = a.nd.kind == VSR_NODATA_VALUE;
+  const int64_t ndv = a.nd.iv;
+  uint32_t colm = 0u;  // elements of the group inside [0, W)
+#pragma unroll
+  for (int e = 0; e < 4; ++e) colm |= static_cast<uint32_t>(xs + e >= 0 && xs + e < a.W) << e;
+  // one vector load per group inside the raster, element loads for the
+  // group that straddles column W
+  const bool ld = xs >= 0 && xs < a.W, whole = xs >= 0 && xs + 4 <= a.W;
+  const bool out_lane = lane >= 1 && lane <= kBwLanes;
+
+  auto load = [&](int i) -> V4 {
+    const int64_t gy = ys - R + i;
+    V4 v{};
+    if (ld && i < nin && gy >= 0 && gy < a.H) {
+      const T* rp = src + gy * a.pitch + xs;
+      if (whole) {
+        v = __ldg(reinterpret_cast<const V4*>(rp));
+      } else {
+        uint32_t e[4] = {0u, 0u, 0u, 0u};
+        for (int q = 0; q < 4 && xs + q < a.W; ++q)
+          e[q] = static_cast<uint32_t>(static_cast<std::make_unsigned_t<T>>(__ldg(rp + q)));
+        if constexpr (sizeof(T) == 1) v = e[0] | (e[1] << 8) | (e[2] << 16) | (e[3] << 24);
+        else v = make_uint2(e[0] | (e[1] << 16), e[2] | (e[3] << 16));
+      }
+    }
+    return v;
+  };
+  V4 pre[P];
+#pragma unroll
+  for (int u = 0; u < P; ++u) pre[u] = load(u);
+  uint32_t hs[P][4];  // horizontal sums of the last P rows (ring slot = row % P)
+  uint32_t vm[P];     // their centre-validity bits
+#pragma unroll
+  for (int u = 0; u < P; ++u) {
+    vm[u] = 0u;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) hs[u][c] = 0u;
+  }
+  uint32_t V[4] = {0u, 0u, 0u, 0u};
+  const float ndf = static_cast<float>(a.nd_out);
+  for (int g0 = 0; g0 < nin; g0 += P) {
+#pragma unroll
+    for (int u = 0; u < P; ++u) {
+      const int i = g0 + u;
+      if (i >= nin) break;
+      const V4 raw = pre[u];
+      pre[u] = load(i + P);
+      const int64_t gy = ys - R + i;
+      const bool rowin = gy >= 0 && gy < a.H;
+      uint32_t e4[4];
+      if constexpr (sizeof(T) == 1) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) e4[e] = (raw >> (8 * e)) & 0xFFu;
+      } else {
+        e4[0] = raw.x & 0xFFFFu;
+        e4[1] = raw.x >> 16;
+        e4[2] = raw.y & 0xFFFFu;
+        e4[3] = raw.y >> 16;
+      }
+      uint32_t w[12];  // left neighbour's 4 words, this lane's, the right neighbour's
+      uint32_t m = 0u;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const T t = static_cast<T>(e4[e]);
+        const bool ok = rowin && ((colm >> e) & 1u) && !(has_nd && static_cast<int64_t>(t) == ndv);
+        w[4 + e] = ok ? (static_cast<uint32_t>(static_cast<int>(t) + OFF) | kOne) : 0u;
+        m |= static_cast<uint32_t>(ok) << e;
+      }
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        w[e] = __shfl_up_sync(0xffffffffu, w[4 + e], 1);
+        w[8 + e] = __shfl_down_sync(0xffffffffu, w[4 + e], 1);
+      }
+      uint32_t h = 0u;
+#pragma unroll
+      for (int j = 4 - R; j <= 4 + R; ++j) h += w[j];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        if (c > 0) h += w[4 + c + R] - w[3 + c - R];
+        V[c] += h - hs[u][c];
+        hs[u][c] = h;
+      }
+      vm[u] = m;
+      if (i >= 2 * R && out_lane) {
+        const uint32_t cm = vm[(u + P - R) % P];  // the centre row i - R
+        const int64_t o = (ys + i - 2 * R) * a.out_pitch + xs;
+        if (a.out_dtype == VSR_F64) {
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const int cnt = static_cast<int>(V[c] >> Pk::kShift);
+            const int sum = static_cast<int>(V[c] & kLow) - OFF * cnt;
+            if (xs + c < a.W)
+              static_cast<double*>(dst)[o + c] =
+                  ((cm >> c) & 1u) ? static_cast<double>(sum) / static_cast<double>(cnt) : a.nd_out;
+          }
+        } else {
+          float q[4];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const uint32_t cnt = V[c] >> Pk::kShift;
+            const float2 t = tab[cnt];
+            // the value sum as a float (exact below 2^23), less the offset
+            const float fs = fmaf(-static_cast<float>(OFF), t.y,
+                                  __uint_as_float(0x4B000000u | (V[c] & kLow)) - 8388608.0f);
+            const float q0 = fs * t.x;
+            q[c] = ((cm >> c) & 1u) ? fmaf(fmaf(-q0, t.y, fs), t.x, q0) : ndf;
+          }
+          float* op = static_cast<float*>(dst) + o;
+          if (VOUT && xs + 3 < a.W) {
+            *reinterpret_cast<float4*>(op) = make_float4(q[0], q[1], q[2], q[3]);
+          } else {
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+              if (xs + c < a.W) op[c] = q[c];
+          }
+        }
+      }
+    }
+  }
+}
+
+template <int R, typename T>
+int launch_warp_t(const BoxArgs& a, cudaStream_t st, int bands) {
+  dim3 grid(static_cast<unsigned>((a.W + kBwWarps * kBwCols - 1) / (kBwWarps * kBwCols)),
+            static_cast<unsigned>((a.H + kBwStrip - 1) / kBwStrip), bands);
+  if (grid.y > 65535u) return fail(VSR_ERR_UNSUPPORTED, "raster too tall for the focal mean grid");
+  const bool vout = a.out_dtype == VSR_F32 && aligned(a.dst, 16) && a.out_pitch % 4 == 0 &&
+                    (bands == 1 || a.out_band_stride % 4 == 0);
+  if (vout) box_warp_int<R, T, true><<<grid, 32 * kBwWarps, 0, st>>>(a);
+  else box_warp_int<R, T, false><<<grid, 32 * kBwWarps, 0, st>>>(a);
+  VSR_CUDA_TRY(cudaGetLastError());
+  return VSR_OK;
+}
+
 template <int R, typename T>
 int launch_slide_t(const BoxArgs& a, cudaStream_t st, int bands) {
+  if constexpr (R <= 4) {  // rows aligned to 4 elements: the register-resident form
+    if (aligned(a.src, 4 * sizeof(T)) && a.pitch % 4 == 0 && (bands == 1 || a.band_stride % 4 == 0))
+      return launch_warp_t<R, T>(a, st, bands);
+  }
   const bool pair = sizeof(T) == 2 && aligned(a.src, 4) && a.pitch % 2 == 0 && a.band_stride % 2 == 0;
   dim3 grid(static_cast<unsigned>((a.W + kSlTW - 1) / kSlTW), static_cast<unsigned>((a.H + kSlStrip - 1) / kSlStrip),
             bands);

@@ -26,6 +26,7 @@
 #include <type_traits>
 
 #include "vsr_internal.cuh"
+#include "df_round.h"
 
 namespace vsr {
 namespace {
@@ -88,8 +89,20 @@ __device__ __forceinline__ void store_out(void* base, int out_dtype, int64_t i, 
   if (out_dtype == VSR_F64) static_cast<double*>(base)[i] = static_cast<double>(v);
   else static_cast<float*>(base)[i] = static_cast<float>(v);
 }
+// hi + lo as a double: both floats widened with integer operations
+// (vsr_f32_widen), one FP64 add; subnormal or non-finite parts convert in FP64.
+__device__ __forceinline__ double df_to_double(float hi, float lo) {
+  const uint32_t hb = __float_as_uint(hi), lb = __float_as_uint(lo);
+  if (!(vsr_f32_widen_ok(hb) && vsr_f32_widen_ok(lb))) return static_cast<double>(hi) + static_cast<double>(lo);
+  uint32_t hh, hl, lh, ll;
+  vsr_f32_widen(hb, &hh, &hl);
+  vsr_f32_widen(lb, &lh, &ll);
+  return __hiloint2double(static_cast<int>(hh), static_cast<int>(hl)) +
+         __hiloint2double(static_cast<int>(lh), static_cast<int>(ll));
+}
+
 __device__ __forceinline__ void store_df(void* base, int out_dtype, int64_t i, DF v) {
-  if (out_dtype == VSR_F64) static_cast<double*>(base)[i] = static_cast<double>(v.hi) + static_cast<double>(v.lo);
+  if (out_dtype == VSR_F64) static_cast<double*>(base)[i] = df_to_double(v.hi, v.lo);
   else static_cast<float*>(base)[i] = v.hi + v.lo;
 }
 

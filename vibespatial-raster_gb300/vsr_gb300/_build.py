@@ -60,7 +60,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_verbose: bool = Fals
     """Compile and link libvsr.so; returns its path."""
     BUILD_DIR.mkdir(parents=True, exist_ok=True)
     sources = sorted(SRC_DIR.glob("*.cu"))
-    headers = sorted(SRC_DIR.glob("*.cuh")) + sorted(INCLUDE_DIR.glob("*.h"))
+    headers = sorted(SRC_DIR.glob("*.cuh")) + sorted(SRC_DIR.glob("*.h")) + sorted(INCLUDE_DIR.glob("*.h"))
     extra = ["-Xptxas=-v"] if ptxas_verbose else []
     jobs = []
     for src in sources:
