@@ -3,10 +3,11 @@
 The reference Gaussian (algebra.py:2120-2154) is the normalised correlation
 with weights outer(g, g) / sum; the oracle evaluates it densely in float64.
 The tensor-core passes split the weights and the row pass's float32 sums into
-F16 hi/lo pairs and drop only the lo*lo products: the bound asserted here is
-2e-6 relative -- |out - ref| <= 2e-6 * max(|ref|, scale), ``scale`` the mean
-|value| of the input -- with nodata placement exact.  Integer values are
-split exactly (at most 16 significant bits).
+F16 hi/lo pairs; the row pass multiplies both weight parts with the exact
+byte planes of the integer values (v = 256 h + l), the column pass drops only
+its lo*lo products: the bound asserted here is 2e-6 relative --
+|out - ref| <= 2e-6 * max(|ref|, scale), ``scale`` the mean |value| of the
+input -- with nodata placement exact.
 """
 
 from __future__ import annotations
@@ -53,6 +54,10 @@ def _raster(dtype, shape, nodata, seed):
     (np.uint8, 255, (257, 190), 49),
     (np.int16, -9999, (190, 257), 65),    # negative values, nodata inside the value range
     (np.uint16, 0, (70, 66), 15),         # kernel larger than a quarter of the raster
+    (np.uint16, 0, (65, 129), 65),        # row-pass tile past the last 64-column block; 1 row past a line block
+    (np.uint8, 0, (97, 60), 3),           # narrower than one row-pass tile; smallest kernel (window lead 8)
+    (np.uint16, 0, (97, 131), 41),        # odd width: rows copied to an aligned pitch first
+    (np.int16, -32768, (140, 700), 79),   # several row-pass tiles per line, signed high bytes
 ])
 def test_split_bf16_gaussian_vs_oracle(vsr, dtype, nodata, shape, k):
     d = _raster(dtype, shape, nodata, k + shape[0])

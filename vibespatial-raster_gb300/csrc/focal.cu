@@ -1217,12 +1217,15 @@ __global__ void __launch_bounds__(32 * kBwWarps) box_warp_int(const BoxArgs a) {
   using Pk = SlidePack<R>;
   using V4 = typename Vec4Of<T>::type;
   constexpr int P = 2 * R + 1;
+  constexpr bool kByte = sizeof(T) == 1;
   constexpr int OFF = std::is_signed<T>::value ? 32768 : 0;
   constexpr uint32_t kOne = 1u << Pk::kShift, kLow = kOne - 1u;
-  static_assert(Pk::kShift <= 23, "value sums must stay below 2^23 for the float conversion");
-  __shared__ float2 tab[Pk::kTaps + 1];  // (RN(1/n), n)
+  static_assert(Pk::kShift >= 16 && Pk::kShift <= 23, "the count bit sits in byte 2; value sums stay below 2^23");
+  // int16 values + 32768 = their bits with bit 15 flipped
+  constexpr uint32_t kFlip = OFF ? 0x80008000u : 0u;
+  __shared__ float2 tab[Pk::kTaps + 1];  // (RN(1/n), -n)
   for (int i = threadIdx.x; i <= Pk::kTaps; i += blockDim.x)
-    tab[i] = make_float2(i ? __frcp_rn(static_cast<float>(i)) : 0.0f, static_cast<float>(i));
+    tab[i] = make_float2(i ? __frcp_rn(static_cast<float>(i)) : 0.0f, -static_cast<float>(i));
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int64_t xw = (static_cast<int64_t>(blockIdx.x) * kBwWarps + (threadIdx.x >> 5)) * kBwCols;
@@ -1234,27 +1237,37 @@ __global__ void __launch_bounds__(32 * kBwWarps) box_warp_int(const BoxArgs a) {
   const int nout = static_cast<int>(a.H - ys < kBwStrip ? a.H - ys : kBwStrip);
   const int nin = nout + 2 * R;  // input rows ys - R .. ys + nout + R - 1
   const bool has_nd = a.nd.kind == VSR_NODATA_VALUE;
-  const int64_t ndv = a.nd.iv;
-  uint32_t colm = 0u;  // elements of the group inside [0, W)
+  // the nodata value's bit pattern in every element slot of a word
+  const uint32_t ndp = static_cast<uint32_t>(a.nd.iv) & (kByte ? 0xFFu : 0xFFFFu);
+  const uint32_t nd_word = kByte ? ndp * 0x01010101u : ndp * 0x00010001u;
+  // elements of the group inside [0, W), as byte (8-bit) or half-word masks
+  // of the two words; one vector load per group inside the raster, element
+  // loads for the group that straddles column W
+  uint32_t cmx = 0u, cmy = 0u;
 #pragma unroll
-  for (int e = 0; e < 4; ++e) colm |= static_cast<uint32_t>(xs + e >= 0 && xs + e < a.W) << e;
-  // one vector load per group inside the raster, element loads for the
-  // group that straddles column W
+  for (int e = 0; e < 4; ++e) {
+    const uint32_t in = (xs + e >= 0 && xs + e < a.W) ? 1u : 0u;
+    if (kByte) cmx |= (in * 0xFFu) << (8 * e);
+    else if (e < 2) cmx |= (in * 0xFFFFu) << (16 * e);
+    else cmy |= (in * 0xFFFFu) << (16 * (e - 2));
+  }
   const bool ld = xs >= 0 && xs < a.W, whole = xs >= 0 && xs + 4 <= a.W;
   const bool out_lane = lane >= 1 && lane <= kBwLanes;
+  const bool f64 = a.out_dtype == VSR_F64;
 
-  auto load = [&](int i) -> V4 {
-    const int64_t gy = ys - R + i;
+  // input row i is raster row ys - R + i; its pointer steps by the pitch
+  const T* rp = src + (ys - R) * a.pitch + xs;
+  auto load = [&](int i, const T* p) -> V4 {
+    const uint64_t gy = static_cast<uint64_t>(ys - R + i);
     V4 v{};
-    if (ld && i < nin && gy >= 0 && gy < a.H) {
-      const T* rp = src + gy * a.pitch + xs;
+    if (ld && i < nin && gy < static_cast<uint64_t>(a.H)) {
       if (whole) {
-        v = __ldg(reinterpret_cast<const V4*>(rp));
+        v = __ldg(reinterpret_cast<const V4*>(p));
       } else {
         uint32_t e[4] = {0u, 0u, 0u, 0u};
         for (int q = 0; q < 4 && xs + q < a.W; ++q)
-          e[q] = static_cast<uint32_t>(static_cast<std::make_unsigned_t<T>>(__ldg(rp + q)));
-        if constexpr (sizeof(T) == 1) v = e[0] | (e[1] << 8) | (e[2] << 16) | (e[3] << 24);
+          e[q] = static_cast<uint32_t>(static_cast<std::make_unsigned_t<T>>(__ldg(p + q)));
+        if constexpr (kByte) v = e[0] | (e[1] << 8) | (e[2] << 16) | (e[3] << 24);
         else v = make_uint2(e[0] | (e[1] << 16), e[2] | (e[3] << 16));
       }
     }
@@ -1262,9 +1275,10 @@ __global__ void __launch_bounds__(32 * kBwWarps) box_warp_int(const BoxArgs a) {
   };
   V4 pre[P];
 #pragma unroll
-  for (int u = 0; u < P; ++u) pre[u] = load(u);
+  for (int u = 0; u < P; ++u) pre[u] = load(u, rp + u * a.pitch);
+  const T* lp = rp + P * a.pitch;  // the row P ahead
   uint32_t hs[P][4];  // horizontal sums of the last P rows (ring slot = row % P)
-  uint32_t vm[P];     // their centre-validity bits
+  uint32_t vm[P];     // their validity, one byte per element (0xFF valid)
 #pragma unroll
   for (int u = 0; u < P; ++u) {
     vm[u] = 0u;
@@ -1273,33 +1287,52 @@ __global__ void __launch_bounds__(32 * kBwWarps) box_warp_int(const BoxArgs a) {
   }
   uint32_t V[4] = {0u, 0u, 0u, 0u};
   const float ndf = static_cast<float>(a.nd_out);
+  int64_t orow = ys * a.out_pitch + xs;  // output row i - 2R
+  // correctly rounded sum / count for two columns: q0 = fs / n by the
+  // reciprocal, one FMA residual correction (exact integers in float32)
+  auto quot2 = [&](uint32_t va, uint32_t vb) -> float2 {
+    const float2 ta = tab[va >> Pk::kShift], tb = tab[vb >> Pk::kShift];
+    float2 fs = __fadd2_rn(make_float2(__uint_as_float(0x4B000000u | (va & kLow)), __uint_as_float(0x4B000000u | (vb & kLow))),
+                           make_float2(-8388608.0f, -8388608.0f));
+    const float2 rn = make_float2(ta.x, tb.x), nn = make_float2(ta.y, tb.y);
+    if (OFF) fs = __ffma2_rn(make_float2(static_cast<float>(OFF), static_cast<float>(OFF)), nn, fs);
+    const float2 q0 = __fmul2_rn(fs, rn);
+    return __ffma2_rn(__ffma2_rn(q0, nn, fs), rn, q0);
+  };
   for (int g0 = 0; g0 < nin; g0 += P) {
 #pragma unroll
     for (int u = 0; u < P; ++u) {
       const int i = g0 + u;
       if (i >= nin) break;
       const V4 raw = pre[u];
-      pre[u] = load(i + P);
-      const int64_t gy = ys - R + i;
-      const bool rowin = gy >= 0 && gy < a.H;
-      uint32_t e4[4];
-      if constexpr (sizeof(T) == 1) {
-#pragma unroll
-        for (int e = 0; e < 4; ++e) e4[e] = (raw >> (8 * e)) & 0xFFu;
-      } else {
-        e4[0] = raw.x & 0xFFFFu;
-        e4[1] = raw.x >> 16;
-        e4[2] = raw.y & 0xFFFFu;
-        e4[3] = raw.y >> 16;
-      }
+      pre[u] = load(i + P, lp);
+      lp += a.pitch;
+      const uint32_t rowm = static_cast<uint64_t>(ys - R + i) < static_cast<uint64_t>(a.H) ? 0xFFFFFFFFu : 0u;
+      // packed words: the element (plus the offset) in bits 0-15, the count
+      // bit above, or 0 where invalid -- byte permutes of the raw words
       uint32_t w[12];  // left neighbour's 4 words, this lane's, the right neighbour's
-      uint32_t m = 0u;
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const T t = static_cast<T>(e4[e]);
-        const bool ok = rowin && ((colm >> e) & 1u) && !(has_nd && static_cast<int64_t>(t) == ndv);
-        w[4 + e] = ok ? (static_cast<uint32_t>(static_cast<int>(t) + OFF) | kOne) : 0u;
-        m |= static_cast<uint32_t>(ok) << e;
+      uint32_t m;      // validity, one byte per element
+      if constexpr (kByte) {
+        const uint32_t x = raw;
+        uint32_t k = cmx & rowm;
+        if (has_nd) k &= ~__vcmpeq4(x, nd_word);
+        m = k;
+        w[4] = __byte_perm(x, kOne, 0x7640) & __byte_perm(k, 0u, 0x0000);
+        w[5] = __byte_perm(x, kOne, 0x7641) & __byte_perm(k, 0u, 0x1111);
+        w[6] = __byte_perm(x, kOne, 0x7642) & __byte_perm(k, 0u, 0x2222);
+        w[7] = __byte_perm(x, kOne, 0x7643) & __byte_perm(k, 0u, 0x3333);
+      } else {
+        const uint32_t x = raw.x, y = raw.y;  // (v0 | v1 << 16), (v2 | v3 << 16)
+        uint32_t kx = cmx & rowm, ky = cmy & rowm;
+        if (has_nd) {
+          kx &= ~__vcmpeq2(x, nd_word);
+          ky &= ~__vcmpeq2(y, nd_word);
+        }
+        m = __byte_perm(kx, ky, 0x6420);
+        w[4] = __byte_perm(x ^ kFlip, kOne, 0x7610) & __byte_perm(kx, 0u, 0x1010);
+        w[5] = __byte_perm(x ^ kFlip, kOne, 0x7632) & __byte_perm(kx, 0u, 0x3232);
+        w[6] = __byte_perm(y ^ kFlip, kOne, 0x7610) & __byte_perm(ky, 0u, 0x1010);
+        w[7] = __byte_perm(y ^ kFlip, kOne, 0x7632) & __byte_perm(ky, 0u, 0x3232);
       }
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
@@ -1316,39 +1349,33 @@ __global__ void __launch_bounds__(32 * kBwWarps) box_warp_int(const BoxArgs a) {
         hs[u][c] = h;
       }
       vm[u] = m;
-      if (i >= 2 * R && out_lane) {
-        const uint32_t cm = vm[(u + P - R) % P];  // the centre row i - R
-        const int64_t o = (ys + i - 2 * R) * a.out_pitch + xs;
-        if (a.out_dtype == VSR_F64) {
+      if (i >= 2 * R) {
+        if (out_lane) {
+          const uint32_t cm = vm[(u + P - R) % P];  // the centre row i - R
+          if (f64) {
 #pragma unroll
-          for (int c = 0; c < 4; ++c) {
-            const int cnt = static_cast<int>(V[c] >> Pk::kShift);
-            const int sum = static_cast<int>(V[c] & kLow) - OFF * cnt;
-            if (xs + c < a.W)
-              static_cast<double*>(dst)[o + c] =
-                  ((cm >> c) & 1u) ? static_cast<double>(sum) / static_cast<double>(cnt) : a.nd_out;
-          }
-        } else {
-          float q[4];
-#pragma unroll
-          for (int c = 0; c < 4; ++c) {
-            const uint32_t cnt = V[c] >> Pk::kShift;
-            const float2 t = tab[cnt];
-            // the value sum as a float (exact below 2^23), less the offset
-            const float fs = fmaf(-static_cast<float>(OFF), t.y,
-                                  __uint_as_float(0x4B000000u | (V[c] & kLow)) - 8388608.0f);
-            const float q0 = fs * t.x;
-            q[c] = ((cm >> c) & 1u) ? fmaf(fmaf(-q0, t.y, fs), t.x, q0) : ndf;
-          }
-          float* op = static_cast<float*>(dst) + o;
-          if (VOUT && xs + 3 < a.W) {
-            *reinterpret_cast<float4*>(op) = make_float4(q[0], q[1], q[2], q[3]);
+            for (int c = 0; c < 4; ++c) {
+              const int cnt = static_cast<int>(V[c] >> Pk::kShift);
+              const int sum = static_cast<int>(V[c] & kLow) - OFF * cnt;
+              if (xs + c < a.W)
+                static_cast<double*>(dst)[orow + c] =
+                    ((cm >> (8 * c)) & 1u) ? static_cast<double>(sum) / static_cast<double>(cnt) : a.nd_out;
+            }
           } else {
+            const float2 q01 = quot2(V[0], V[1]), q23 = quot2(V[2], V[3]);
+            const float q[4] = {(cm & 1u) ? q01.x : ndf, ((cm >> 8) & 1u) ? q01.y : ndf,
+                                ((cm >> 16) & 1u) ? q23.x : ndf, ((cm >> 24) & 1u) ? q23.y : ndf};
+            float* op = static_cast<float*>(dst) + orow;
+            if (VOUT && xs + 3 < a.W) {
+              *reinterpret_cast<float4*>(op) = make_float4(q[0], q[1], q[2], q[3]);
+            } else {
 #pragma unroll
-            for (int c = 0; c < 4; ++c)
-              if (xs + c < a.W) op[c] = q[c];
+              for (int c = 0; c < 4; ++c)
+                if (xs + c < a.W) op[c] = q[c];
+            }
           }
         }
+        orow += a.out_pitch;
       }
     }
   }
