@@ -448,10 +448,11 @@ __global__ void __launch_bounds__(kRThreads, 1) gauss_row_kernel(const GaussArgs
           cm0 = (in(3) ? 0x0000FFFFu : 0u) | (in(2) ? 0xFFFF0000u : 0u);
           cm1 = (in(1) ? 0x0000FFFFu : 0u) | (in(0) ? 0xFFFF0000u : 0u);
         }
+        const int64_t left = a.lines - l0 - cw;  // this warp's lines inside the raster: q * 8 < left
 #pragma unroll
         for (int q = 0; q < kLinesPerWarp; ++q) {
           uint32_t keep0 = cm0, keep1 = cm1;
-          if (l0 + cw + kRWarps * q >= a.lines) keep0 = keep1 = 0u;
+          if (kRWarps * q >= left) keep0 = keep1 = 0u;
           uint32_t h0, h1, l0w, l1w;
           if (kEsz == 1) {
             const uint32_t x = raw[q][h].x;  // bytes v0 .. v3
@@ -527,9 +528,14 @@ __global__ void __launch_bounds__(kRThreads, 1) gauss_row_kernel(const GaussArgs
 #pragma unroll
           for (int e = 0; e < 8; ++e) {
             const int n = 8 * c2 + e;
-            const bool keep = xin && y0 + e < a.lines;
-            num[e] = keep ? fmaf(__uint_as_float(rh[n]), 0.03125f, __uint_as_float(rl[n]) * 0.0001220703125f) : 0.0f;
-            den[e] = keep ? __uint_as_float(rv[n]) * 0.0625f : 0.0f;
+            num[e] = fmaf(__uint_as_float(rh[n]), 0.03125f, __uint_as_float(rl[n]) * 0.0001220703125f);
+            den[e] = __uint_as_float(rv[n]) * 0.0625f;
+          }
+          if (!xin || y0 + 8 > a.lines) {  // rows past the raster, or a column past it: zeros
+            const int nrow = xin ? static_cast<int>(a.lines - y0) : 0;
+#pragma unroll
+            for (int e = 0; e < 8; ++e)
+              if (e >= nrow) num[e] = den[e] = 0.0f;
           }
           uint4 nh, nl, dh, dl;
           split_row8(num, nh, nl);
