@@ -770,11 +770,11 @@ def leg_multiband(args, dev, gpu) -> dict:
         "gpu_launches": 4,
         "focal_mean_ms": t_mean, "focal_mean_gpix_s": px / (t_mean * 1e-3) / 1e9,
         "focal_mean_hbm_frac": 6 * px / (t_mean * 1e-3) / 1e9 / hbm,
-        "gaussian_path": "auto = split-precision tensor-core line passes (F16 hi/lo, FP32 accumulate)",
+        "gaussian_path": "auto = split-precision tensor-core line passes (row pass: exact byte planes x F16 hi/lo weights; column pass: F16 hi/lo row sums; FP32 accumulate)",
         "gaussian_tensor_core_ms": t_tc, "gaussian_fp32_ms": t_fp32, "gaussian_tensor_core_vs_fp32": t_fp32 / t_tc,
         "l2": "2.9 GB in + 11.6 GB out per step exceed L2; no flush",
         "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                     "peak_source": src, "kernel": "box_slide_int + gauss_line_kernel", "bytes_per_px": 10},
+                     "peak_source": src, "kernel": "box_warp_int + gauss_row_kernel + gauss_col_kernel", "bytes_per_px": 10},
         "cpu_baseline": {"value": 1.0 / (cpu_mean_s + cpu_gauss_s) / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
                          "sample": "band 0: 7x7 focal mean on a 1024^2 crop + 65x65 Gaussian (dense float64 "
                                    "correlate, as the reference's dense kernel) on a 256^2 crop, per-pixel times "
