@@ -148,3 +148,35 @@ def test_focal_stats_bands_one_launch(vsr):
         assert out.shape == stack.shape
         for b in range(3):
             _check(out[b], oracle.focal_stat(stack[b], 2, 2, 7, stat), stack[b], stat, f"band {b}")
+
+
+@pytest.mark.parametrize("dtype", [np.uint8, np.int16, np.uint16])
+@pytest.mark.parametrize("r", [1, 2, 3, 4])
+def test_focal_stats_register_resident_kernel(vsr, dtype, r):
+    """8/16-bit rasters whose rows are aligned to 4 elements take the
+    register-resident min / max / range kernel for square radii up to 4:
+    120-column warp strips (ragged at 964 = 2 x 480 + 4 columns), 256-row
+    strips, a raster narrower than a lane group, signed values; outputs equal
+    to the oracle (float64 and float32).  The 8/16-bit std with a float32
+    output is sqrt(n^2 var)/n rounded once to float32: within one float32 ulp
+    of the float64 oracle, equal to it rounded on (nearly) every pixel."""
+    rng = np.random.default_rng(100 * r + np.dtype(dtype).itemsize)
+    lo, hi = {np.uint8: (0, 254), np.int16: (-32767, 32767), np.uint16: (0, 65534)}[dtype]
+    nd = {np.uint8: 255, np.int16: -32768, np.uint16: 65535}[dtype]
+    for shape in [(530, 964), (300, 1024), (9, 4)]:
+        d = rng.integers(lo, hi, shape, endpoint=True).astype(dtype)
+        d[rng.random(shape) < 0.03] = nd
+        d[:12, :14] = nd  # empty windows
+        for stat in ("min", "max", "range"):
+            ref = oracle.focal_stat(d, r, r, nd, stat)
+            _check(_run(vsr, d, nd, stat, r).to_numpy(), ref, d, stat, f"{shape} r{r}")
+            out32 = _run(vsr, d, nd, stat, r, out_dtype=np.float32).to_numpy()
+            np.testing.assert_array_equal(out32, ref.astype(np.float32), err_msg=f"{shape} r{r} {stat} f32")
+        ref = oracle.focal_stat(d, r, r, nd, "std")
+        out32 = _run(vsr, d, nd, "std", r, out_dtype=np.float32).to_numpy()
+        r32 = ref.astype(np.float32)
+        m = ~np.isnan(ref)
+        np.testing.assert_array_equal(np.isnan(out32), np.isnan(r32))
+        ulp = np.abs(out32[m].view(np.int32).astype(np.int64) - r32[m].view(np.int32).astype(np.int64))
+        assert ulp.max() <= 1, f"{shape} r{r} std f32 ulp {ulp.max()}"
+        assert (ulp == 0).mean() >= 0.9999

@@ -11,12 +11,17 @@
 //              makes the result NaN;
 //   range      max - min of the valid taps (nodata and NaN excluded);
 //   std        population standard deviation of the valid taps; 0.0 for an
-//              empty window;
+//              empty window (8/16-bit rasters: exact integer sums, and for a
+//              float32 output sqrt(n^2 var)/n rounded once to float32 by
+//              vsr_std_f32, std_round.h);
 //   variety    number of distinct valid values; 0 for an empty window.
 // An empty window gives the raster's nodata value (0.0 when it has none), a
 // nodata centre gives the nodata value.
 //
-// A CTA owns a 64 x 16 output tile and stages its (16 + 2ry) x (64 + 2rx)
+// For 8/16-bit rasters with square windows of radius <= 4 and rows aligned to
+// 4 elements, min / max / range run in fs_warp_kernel (register-resident,
+// below); everything else in focal_stat_kernel:
+// a CTA owns a 64 x 16 output tile and stages its (16 + 2ry) x (64 + 2rx)
 // input window into shared memory, converted once to the statistic's type
 // (float for 8/16-bit and float32 rasters, double for int32 / float64,
 // int32 for the integer std), nodata and out-of-bounds taps already replaced
@@ -31,6 +36,7 @@
 #include <type_traits>
 
 #include "vsr_internal.cuh"
+#include "std_round.h"
 
 namespace vsr {
 namespace {
@@ -240,7 +246,16 @@ __global__ void __launch_bounds__(kFsThreads) focal_stat_kernel(const FsArgs a) 
           q += Rq[(r + d) * kFsTX + c];
           n += Rn[(r + d) * kFsTX + c];
         }
-        out_at(r, c, n ? sqrt(static_cast<double>(static_cast<int64_t>(n) * q - sm * sm)) / n : 0.0);
+        const int64_t num = static_cast<int64_t>(n) * q - sm * sm;  // n^2 var, exact
+        if (a.out_dtype == VSR_F32) {
+          // float32 output: sqrt(num)/n correctly rounded without FP64
+          const int64_t y = y0 + r, x = x0 + c;
+          reinterpret_cast<float*>(obase)[y * a.out_pitch + x] =
+              ndc[r * kFsTX + c] ? static_cast<float>(a.nd_out)
+                                 : (n ? vsr_std_f32(static_cast<uint64_t>(num), static_cast<uint32_t>(n)) : 0.0f);
+        } else {
+          out_at(r, c, n ? sqrt(static_cast<double>(num)) / n : 0.0);
+        }
       }
   } else {
     for (int r = warp; r < nr; r += WARPS)
@@ -290,6 +305,215 @@ __global__ void __launch_bounds__(kFsThreads) focal_stat_kernel(const FsArgs a) 
   }
 }
 
+// ---------------------------------------------- register-resident min / max / range
+// 8/16-bit rasters, square (2R+1)^2 windows with R <= 4, rows aligned to 4
+// elements: the warp-strip form of the integer focal mean (focal.cu,
+// box_warp_int).  A warp owns a 128-column strip, 4 columns per lane (lanes
+// 0 and 31 only supply neighbours: 120 output columns per warp); per input
+// row each lane loads its 4 elements (prefetched 2R+1 rows ahead), turns
+// them into order-preserving keys (int16: bit 15 flipped), invalid taps
+// (nodata, outside the raster) made neutral -- 0x10000 for the minimum,
+// 0 for the maximum, whose valid keys are v + 1 -- takes R keys from each
+// neighbour by shuffles, reduces its 4 horizontal windows, and reduces the
+// last 2R+1 rows' results over a register ring (the row loop unrolled by
+// 2R+1).  An empty window (minimum key 0x10000 / maximum key 0) or a nodata
+// centre gives the nodata value.
+constexpr int kFwLanes = 30;
+constexpr int kFwCols = 4 * kFwLanes;
+constexpr int kFwWarps = 4;
+constexpr int kFwStrip = 256;
+
+template <typename T>
+struct Fw4 {  // 4 elements in one load
+  using type = uint2;
+};
+template <>
+struct Fw4<uint8_t> {
+  using type = uint32_t;
+};
+
+template <int R, typename T, int S, bool VOUT>
+__global__ void __launch_bounds__(32 * kFwWarps) fs_warp_kernel(const FsArgs a) {
+  static_assert(R >= 1 && R <= 4, "the neighbour exchange covers radii up to 4");
+  static_assert(S == VSR_STAT_MIN || S == VSR_STAT_MAX || S == VSR_STAT_RANGE, "min, max or range");
+  using V4 = typename Fw4<T>::type;
+  constexpr int P = 2 * R + 1;
+  constexpr bool kMin = S != VSR_STAT_MAX, kMax = S != VSR_STAT_MIN;
+  constexpr uint32_t kFlip = std::is_signed<T>::value ? 0x8000u : 0u;
+  constexpr uint32_t kMask = sizeof(T) == 1 ? 0xFFu : 0xFFFFu;
+  constexpr uint32_t kNoMin = 0x10000u;
+  const int lane = threadIdx.x & 31;
+  const int64_t xw = (static_cast<int64_t>(blockIdx.x) * kFwWarps + (threadIdx.x >> 5)) * kFwCols;
+  if (xw >= a.W) return;
+  const int64_t xs = xw - 4 + 4 * lane;
+  const int64_t ys = static_cast<int64_t>(blockIdx.y) * kFwStrip;
+  const T* src = static_cast<const T*>(a.src) + static_cast<int64_t>(blockIdx.z) * a.band_stride;
+  char* obase = static_cast<char*>(a.dst) +
+                static_cast<int64_t>(blockIdx.z) * a.out_band_stride * (a.out_dtype == VSR_F64 ? 8 : 4);
+  const int nout = static_cast<int>(a.H - ys < kFwStrip ? a.H - ys : kFwStrip);
+  const int nin = nout + 2 * R;
+  const bool has_nd = a.kind == VSR_NODATA_VALUE;
+  const uint32_t ndk = static_cast<uint32_t>(static_cast<int64_t>(a.ndv)) & kMask;  // nodata's bit pattern
+  uint32_t colm = 0u;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) colm |= static_cast<uint32_t>(xs + e >= 0 && xs + e < a.W) << e;
+  const bool ld = xs >= 0 && xs < a.W, whole = xs >= 0 && xs + 4 <= a.W;
+  const bool out_lane = lane >= 1 && lane <= kFwLanes;
+  const bool f64 = a.out_dtype == VSR_F64;
+  const T* rp = src + (ys - R) * a.pitch + xs;
+  auto load = [&](int i, const T* p) -> V4 {
+    const uint64_t gy = static_cast<uint64_t>(ys - R + i);
+    V4 v{};
+    if (ld && i < nin && gy < static_cast<uint64_t>(a.H)) {
+      if (whole) {
+        v = __ldg(reinterpret_cast<const V4*>(p));
+      } else {
+        uint32_t e[4] = {0u, 0u, 0u, 0u};
+        for (int q = 0; q < 4 && xs + q < a.W; ++q)
+          e[q] = static_cast<uint32_t>(static_cast<std::make_unsigned_t<T>>(__ldg(p + q)));
+        if constexpr (sizeof(T) == 1) v = e[0] | (e[1] << 8) | (e[2] << 16) | (e[3] << 24);
+        else v = make_uint2(e[0] | (e[1] << 16), e[2] | (e[3] << 16));
+      }
+    }
+    return v;
+  };
+  V4 pre[P];
+#pragma unroll
+  for (int u = 0; u < P; ++u) pre[u] = load(u, rp + u * a.pitch);
+  const T* lp = rp + P * a.pitch;
+  uint32_t hmn[P][4], hmx[P][4], vm[P];  // per row: horizontal min / max keys, validity bits
+#pragma unroll
+  for (int u = 0; u < P; ++u) {
+    vm[u] = 0u;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      hmn[u][c] = kNoMin;
+      hmx[u][c] = 0u;
+    }
+  }
+  int64_t orow = ys * a.out_pitch + xs;
+  for (int g0 = 0; g0 < nin; g0 += P) {
+#pragma unroll
+    for (int u = 0; u < P; ++u) {
+      const int i = g0 + u;
+      if (i >= nin) break;
+      const V4 raw = pre[u];
+      pre[u] = load(i + P, lp);
+      lp += a.pitch;
+      const bool rowin = static_cast<uint64_t>(ys - R + i) < static_cast<uint64_t>(a.H);
+      uint32_t e4[4];
+      if constexpr (sizeof(T) == 1) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) e4[e] = (raw >> (8 * e)) & 0xFFu;
+      } else {
+        e4[0] = raw.x & 0xFFFFu;
+        e4[1] = raw.x >> 16;
+        e4[2] = raw.y & 0xFFFFu;
+        e4[3] = raw.y >> 16;
+      }
+      uint32_t kmn[12], kmx[12], m = 0u;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const bool ok = rowin && ((colm >> e) & 1u) && !(has_nd && e4[e] == ndk);
+        const uint32_t key = e4[e] ^ kFlip;
+        kmn[4 + e] = ok ? key : kNoMin;
+        kmx[4 + e] = ok ? key + 1u : 0u;
+        m |= static_cast<uint32_t>(ok) << e;
+      }
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        if (kMin) {
+          kmn[e] = __shfl_up_sync(0xffffffffu, kmn[4 + e], 1);
+          kmn[8 + e] = __shfl_down_sync(0xffffffffu, kmn[4 + e], 1);
+        }
+        if (kMax) {
+          kmx[e] = __shfl_up_sync(0xffffffffu, kmx[4 + e], 1);
+          kmx[8 + e] = __shfl_down_sync(0xffffffffu, kmx[4 + e], 1);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        uint32_t a0 = kNoMin, a1 = 0u;
+#pragma unroll
+        for (int j = 4 + c - R; j <= 4 + c + R; ++j) {
+          if (kMin) a0 = min(a0, kmn[j]);
+          if (kMax) a1 = max(a1, kmx[j]);
+        }
+        hmn[u][c] = a0;
+        hmx[u][c] = a1;
+      }
+      vm[u] = m;
+      if (i >= 2 * R) {
+        if (out_lane) {
+          const uint32_t cm = vm[(u + P - R) % P];  // the centre row i - R
+          float q[4];
+          double qd[4];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            uint32_t mn = kNoMin, mx = 0u;
+#pragma unroll
+            for (int t = 0; t < P; ++t) {
+              if (kMin) mn = min(mn, hmn[t][c]);
+              if (kMax) mx = max(mx, hmx[t][c]);
+            }
+            const bool empty = kMin ? mn == kNoMin : mx == 0u;
+            const bool nd = empty || !((cm >> c) & 1u);
+            // keys back to values: undo the flip (int16 sign-extends)
+            const float vmn = static_cast<float>(static_cast<T>((mn ^ kFlip) & kMask));
+            const float vmx = static_cast<float>(static_cast<T>(((mx - 1u) ^ kFlip) & kMask));
+            const float v = S == VSR_STAT_MIN ? vmn : (S == VSR_STAT_MAX ? vmx : vmx - vmn);  // exact
+            q[c] = nd ? static_cast<float>(a.nd_out) : v;
+            qd[c] = nd ? a.nd_out : static_cast<double>(v);
+          }
+          if (f64) {
+            double* op = reinterpret_cast<double*>(obase) + orow;
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+              if (xs + c < a.W) op[c] = qd[c];
+          } else {
+            float* op = reinterpret_cast<float*>(obase) + orow;
+            if (VOUT && xs + 3 < a.W) {
+              *reinterpret_cast<float4*>(op) = make_float4(q[0], q[1], q[2], q[3]);
+            } else {
+#pragma unroll
+              for (int c = 0; c < 4; ++c)
+                if (xs + c < a.W) op[c] = q[c];
+            }
+          }
+        }
+        orow += a.out_pitch;
+      }
+    }
+  }
+}
+
+template <int R, typename T, int S>
+int fs_warp_launch(const FsArgs& a, int bands, cudaStream_t st) {
+  const dim3 grid(static_cast<unsigned>((a.W + kFwWarps * kFwCols - 1) / (kFwWarps * kFwCols)),
+                  static_cast<unsigned>((a.H + kFwStrip - 1) / kFwStrip), static_cast<unsigned>(bands));
+  if (grid.y > 65535u) return -1;
+  const bool vout = a.out_dtype == VSR_F32 && aligned(a.dst, 16) && a.out_pitch % 4 == 0 &&
+                    (bands == 1 || a.out_band_stride % 4 == 0);
+  if (vout) fs_warp_kernel<R, T, S, true><<<grid, 32 * kFwWarps, 0, st>>>(a);
+  else fs_warp_kernel<R, T, S, false><<<grid, 32 * kFwWarps, 0, st>>>(a);
+  VSR_CUDA_TRY(cudaGetLastError());
+  return VSR_OK;
+}
+
+// The register-resident form when it applies (8/16-bit min / max / range,
+// square window of radius 1..4, rows aligned to 4 elements); -1 otherwise.
+template <typename T, int S>
+int fs_warp_try(const FsArgs& a, int bands, cudaStream_t st) {
+  if (a.ry != a.rx || a.ry < 1 || a.ry > 4) return -1;
+  if (!aligned(a.src, 4 * sizeof(T)) || a.pitch % 4 != 0 || (bands > 1 && a.band_stride % 4 != 0)) return -1;
+  switch (a.ry) {
+    case 1: return fs_warp_launch<1, T, S>(a, bands, st);
+    case 2: return fs_warp_launch<2, T, S>(a, bands, st);
+    case 3: return fs_warp_launch<3, T, S>(a, bands, st);
+    default: return fs_warp_launch<4, T, S>(a, bands, st);
+  }
+}
+
 template <typename TIN, typename T, int S>
 int fs_launch(const FsArgs& a, int bands, cudaStream_t st) {
   const size_t smem = FsLayout<S, T>::total(a.ry, a.rx);
@@ -316,6 +540,16 @@ int fs_dispatch(const FsArgs& a, int bands, cudaStream_t st) {
       default: return fs_launch<double, double, S>(a, bands, st);
     }
   } else {
+    if constexpr (S != VSR_STAT_VARIETY) {
+      int rc = -1;
+      switch (a.dtype) {
+        case VSR_U8: rc = fs_warp_try<uint8_t, S>(a, bands, st); break;
+        case VSR_I16: rc = fs_warp_try<int16_t, S>(a, bands, st); break;
+        case VSR_U16: rc = fs_warp_try<uint16_t, S>(a, bands, st); break;
+        default: break;
+      }
+      if (rc >= 0) return rc;
+    }
     switch (a.dtype) {
       case VSR_U8: return fs_launch<uint8_t, float, S>(a, bands, st);
       case VSR_I16: return fs_launch<int16_t, float, S>(a, bands, st);
