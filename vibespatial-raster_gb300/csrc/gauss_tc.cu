@@ -50,8 +50,8 @@
 // warps 1-8 load each tile's raster window a tile ahead into registers,
 // convert it into a B buffer and run the epilogue two tiles behind the
 // conversion (tile j-1's MMAs overlap tile j's conversion); pass 2: warp 1
-// bulk-copies the A windows in, warps 2-9 copy the centre pixels and run the
-// epilogue.  Operand buffers and TMEM accumulators are double-buffered and
+// bulk-copies the A windows in, warps 2-17 copy the centre pixels and run the
+// epilogue (16 warps: 4 per TMEM lane quarter).  Operand buffers and TMEM accumulators are double-buffered and
 // handed over through mbarriers; every wait is bounded (on expiry an error
 // bit is recorded, a shared abort flag ends the other roles' waits, and the
 // MMA issuer and the copy producer wait for their operations in flight
@@ -74,9 +74,11 @@ using namespace tc;
 // ---- pass 2 (columns) geometry
 constexpr int kGL = kMmaM / 2;        // lines per tile
 constexpr int kGN = kMmaN;            // positions per tile (MMA N)
-constexpr int kGWarps = 8;            // centre-copy / epilogue warps (warps 2..9)
+constexpr int kGWarps = 16;           // centre-copy / epilogue warps (warps 2..17)
 constexpr int kGConv = 32 * kGWarps;  // their threads
 constexpr int kGThreads = 64 + kGConv;
+constexpr int kGPosPart = kGN / (kGWarps / 4);  // positions per epilogue warp (4 warps per TMEM lane quarter)
+constexpr int kGRowStep = kGConv / kGL;         // output rows between a thread's quotients
 constexpr uint32_t kGChunk = kMmaM * 16;  // pass-2 A: one 8-position core-matrix column of 128 rows (2 KB)
 constexpr int kGMaxK = 79;
 constexpr int kGXPitch = kGN + 1;     // pass-2 exchange rows (floats; odd: conflict-free)
@@ -701,7 +703,7 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_col_kernel(const GaussArgs
     // ========================================================= centre copies + epilogue
     const int ct = tid - 64;           // thread 0..255
     const int quarter = warp & 3;      // the TMEM lane quarter this warp may read
-    const int half = (warp - 2) >> 2;  // epilogue: positions 32 half .. +31
+    const int part = (warp - 2) >> 2;  // epilogue: positions kGPosPart part .. + kGPosPart - 1
     const bool nd_val = a.nd_kind == VSR_NODATA_VALUE;
     constexpr int kEsz = DT == VSR_U8 ? 1 : 2;  // raster element bytes
 
@@ -746,10 +748,10 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_col_kernel(const GaussArgs
       if (g_any<kGConv>(!got)) return false;
       tc_fence_after();
       const int m = quarter * 32 + lane;
-      const uint32_t lane_base = tmem + b * 2 * kGN + (static_cast<uint32_t>(quarter * 32) << 16) + half * 32;
+      const uint32_t lane_base = tmem + b * 2 * kGN + (static_cast<uint32_t>(quarter * 32) << 16) + part * kGPosPart;
       float* xs = reinterpret_cast<float*>(sm + L.xch);
 #pragma unroll
-      for (int h16 = 0; h16 < 2; ++h16) {
+      for (int h16 = 0; h16 < kGPosPart / 16; ++h16) {
         uint32_t ra_[16], rb_[16];
         tmem_ld16_issue(lane_base + 16 * h16, ra_);
         tmem_ld16_issue(lane_base + kGN + 16 * h16, rb_);
@@ -759,8 +761,8 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_col_kernel(const GaussArgs
         for (int n = 0; n < 16; n += 2) {
           const float2 sum = __fadd2_rn(make_float2(__uint_as_float(ra_[n]), __uint_as_float(ra_[n + 1])),
                                         make_float2(__uint_as_float(rb_[n]), __uint_as_float(rb_[n + 1])));
-          xs[m * kGXPitch + half * 32 + 16 * h16 + n] = sum.x;
-          xs[m * kGXPitch + half * 32 + 16 * h16 + n + 1] = sum.y;
+          xs[m * kGXPitch + part * kGPosPart + 16 * h16 + n] = sum.x;
+          xs[m * kGXPitch + part * kGPosPart + 16 * h16 + n + 1] = sum.y;
         }
       }
       tc_fence_before();
@@ -768,19 +770,19 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_col_kernel(const GaussArgs
       cp_async_wait<2>();          // this thread's centre copies of this tile have landed
       g_sync<kGConv>();
       // output: thread ct takes line i2 (raster column x2) and positions
-      // (rows) ct / 64 + 4 q; a warp's lanes are 32 consecutive x
+      // (rows) ct / 64 + kGRowStep q; a warp's lanes are 32 consecutive x
       // quotient: __fdividef (within 2 ulp; den <= 2^20 here, far below
       // its 2^126 limit), exact power-of-two rescale
       if (x2 < a.lines) {
         const int64_t y0 = p0 + (ct >> 6);
-        const int64_t nrem = (a.len - y0 + 3) / 4;  // rows y0 + 4 q inside the raster
-        const int nq = nrem < kGN / 4 ? static_cast<int>(nrem) : kGN / 4;
+        const int64_t nrem = (a.len - y0 + kGRowStep - 1) / kGRowStep;  // rows y0 + kGRowStep q inside the raster
+        const int nq = nrem < kGN / kGRowStep ? static_cast<int>(nrem) : kGN / kGRowStep;
         if (a.out_dtype == VSR_F64) {
           double* op = static_cast<double*>(a.dst) + bd * a.out_bstride + y0 * a.out_pitch + x2;
 #pragma unroll
-          for (int q = 0; q < kGN / 4; ++q, op += 4 * a.out_pitch) {
+          for (int q = 0; q < kGN / kGRowStep; ++q, op += kGRowStep * a.out_pitch) {
             if (q >= nq) break;
-            const int p = (ct >> 6) + 4 * q;
+            const int p = (ct >> 6) + kGRowStep * q;
             const float num = xs[i2 * kGXPitch + p], den = xs[(kGL + i2) * kGXPitch + p];
             const bool ok = !(nd_val && centre(cb, p, i2) == a.nd_iv) && den > 0.0f;
             *op = ok ? static_cast<double>(__fdividef(num, den) * (kGScaleD / kGScaleV)) : a.nd_out;
@@ -789,9 +791,9 @@ __global__ void __launch_bounds__(kGThreads, 1) gauss_col_kernel(const GaussArgs
           float* op = static_cast<float*>(a.dst) + bd * a.out_bstride + y0 * a.out_pitch + x2;
           const float ndf = static_cast<float>(a.nd_out);
 #pragma unroll
-          for (int q = 0; q < kGN / 4; ++q, op += 4 * a.out_pitch) {
+          for (int q = 0; q < kGN / kGRowStep; ++q, op += kGRowStep * a.out_pitch) {
             if (q >= nq) break;
-            const int p = (ct >> 6) + 4 * q;
+            const int p = (ct >> 6) + kGRowStep * q;
             const float num = xs[i2 * kGXPitch + p], den = xs[(kGL + i2) * kGXPitch + p];
             const bool ok = !(nd_val && centre(cb, p, i2) == a.nd_iv) && den > 0.0f;
             *op = ok ? __fdividef(num, den) * (kGScaleD / kGScaleV) : ndf;
