@@ -1,5 +1,6 @@
-/* Host check of vsr_std_f32 (csrc/std_round.h): for random and edge-case
- * integer pairs (N, n) it must equal sqrt(N)/n correctly rounded to float32,
+/* Host check of vsr_std_f32 and, for n < 128, vsr_std_f32_small
+ * (csrc/std_round.h): for random and edge-case integer pairs (N, n) both must
+ * equal sqrt(N)/n correctly rounded to float32,
  * found here by bracketing with long double and an exact midpoint test.
  * Prints "n mismatches"; exits non-zero on a mismatch. */
 #include <math.h>
@@ -53,6 +54,10 @@ int main(int argc, char** argv) {
       N = (next() >> 20) % ((uint64_t)n * n * 4294967296ull / 4 + 1);
     }
     const float got = vsr_std_f32(N, n), ref = N ? reference(N, n) : 0.0f;
+    if (n < 128 && vsr_std_f32_small(N, n) != ref) {
+      if (bad < 5) printf("small-form mismatch N=%llu n=%u\n", (unsigned long long)N, n);
+      ++bad;
+    }
     if (got != ref) {
       if (bad < 5) printf("mismatch N=%llu n=%u got %.9g ref %.9g\n", (unsigned long long)N, n, got, ref);
       ++bad;

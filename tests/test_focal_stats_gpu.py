@@ -154,7 +154,8 @@ def test_focal_stats_bands_one_launch(vsr):
 @pytest.mark.parametrize("r", [1, 2, 3, 4])
 def test_focal_stats_register_resident_kernel(vsr, dtype, r):
     """8/16-bit rasters whose rows are aligned to 4 elements take the
-    register-resident min / max / range kernel for square radii up to 4:
+    register-resident min / max / range and std kernels for square radii up
+    to 4:
     120-column warp strips (ragged at 964 = 2 x 480 + 4 columns), 256-row
     strips, a raster narrower than a lane group, signed values; outputs equal
     to the oracle (float64 and float32).  The 8/16-bit std with a float32
@@ -173,6 +174,7 @@ def test_focal_stats_register_resident_kernel(vsr, dtype, r):
             out32 = _run(vsr, d, nd, stat, r, out_dtype=np.float32).to_numpy()
             np.testing.assert_array_equal(out32, ref.astype(np.float32), err_msg=f"{shape} r{r} {stat} f32")
         ref = oracle.focal_stat(d, r, r, nd, "std")
+        _check(_run(vsr, d, nd, "std", r).to_numpy(), ref, d, "std", f"{shape} r{r}")
         out32 = _run(vsr, d, nd, "std", r, out_dtype=np.float32).to_numpy()
         r32 = ref.astype(np.float32)
         m = ~np.isnan(ref)

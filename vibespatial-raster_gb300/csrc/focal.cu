@@ -1211,7 +1211,7 @@ struct Vec4Of<uint8_t> {
   using type = uint32_t;
 };
 
-template <int R, typename T, bool VOUT>
+template <int R, typename T, bool VOUT, bool F64>
 __global__ void __launch_bounds__(32 * kBwWarps) box_warp_int(const BoxArgs a) {
   static_assert(R >= 1 && R <= 4, "the neighbour exchange covers radii up to 4");
   using Pk = SlidePack<R>;
@@ -1253,7 +1253,6 @@ __global__ void __launch_bounds__(32 * kBwWarps) box_warp_int(const BoxArgs a) {
   }
   const bool ld = xs >= 0 && xs < a.W, whole = xs >= 0 && xs + 4 <= a.W;
   const bool out_lane = lane >= 1 && lane <= kBwLanes;
-  const bool f64 = a.out_dtype == VSR_F64;
 
   // input row i is raster row ys - R + i; its pointer steps by the pitch
   const T* rp = src + (ys - R) * a.pitch + xs;
@@ -1352,7 +1351,7 @@ __global__ void __launch_bounds__(32 * kBwWarps) box_warp_int(const BoxArgs a) {
       if (i >= 2 * R) {
         if (out_lane) {
           const uint32_t cm = vm[(u + P - R) % P];  // the centre row i - R
-          if (f64) {
+          if constexpr (F64) {
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
               const int cnt = static_cast<int>(V[c] >> Pk::kShift);
@@ -1388,8 +1387,9 @@ int launch_warp_t(const BoxArgs& a, cudaStream_t st, int bands) {
   if (grid.y > 65535u) return fail(VSR_ERR_UNSUPPORTED, "raster too tall for the focal mean grid");
   const bool vout = a.out_dtype == VSR_F32 && aligned(a.dst, 16) && a.out_pitch % 4 == 0 &&
                     (bands == 1 || a.out_band_stride % 4 == 0);
-  if (vout) box_warp_int<R, T, true><<<grid, 32 * kBwWarps, 0, st>>>(a);
-  else box_warp_int<R, T, false><<<grid, 32 * kBwWarps, 0, st>>>(a);
+  if (a.out_dtype == VSR_F64) box_warp_int<R, T, false, true><<<grid, 32 * kBwWarps, 0, st>>>(a);
+  else if (vout) box_warp_int<R, T, true, false><<<grid, 32 * kBwWarps, 0, st>>>(a);
+  else box_warp_int<R, T, false, false><<<grid, 32 * kBwWarps, 0, st>>>(a);
   VSR_CUDA_TRY(cudaGetLastError());
   return VSR_OK;
 }

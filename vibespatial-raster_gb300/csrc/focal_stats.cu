@@ -19,8 +19,8 @@
 // nodata centre gives the nodata value.
 //
 // For 8/16-bit rasters with square windows of radius <= 4 and rows aligned to
-// 4 elements, min / max / range run in fs_warp_kernel (register-resident,
-// below); everything else in focal_stat_kernel:
+// 4 elements, min / max / range run in fs_warp_kernel and std in fs_warp_std
+// (register-resident, below); everything else in focal_stat_kernel:
 // a CTA owns a 64 x 16 output tile and stages its (16 + 2ry) x (64 + 2rx)
 // input window into shared memory, converted once to the statistic's type
 // (float for 8/16-bit and float32 rasters, double for int32 / float64,
@@ -332,7 +332,7 @@ struct Fw4<uint8_t> {
   using type = uint32_t;
 };
 
-template <int R, typename T, int S, bool VOUT>
+template <int R, typename T, int S, bool VOUT, bool F64>
 __global__ void __launch_bounds__(32 * kFwWarps) fs_warp_kernel(const FsArgs a) {
   static_assert(R >= 1 && R <= 4, "the neighbour exchange covers radii up to 4");
   static_assert(S == VSR_STAT_MIN || S == VSR_STAT_MAX || S == VSR_STAT_RANGE, "min, max or range");
@@ -359,7 +359,6 @@ __global__ void __launch_bounds__(32 * kFwWarps) fs_warp_kernel(const FsArgs a) 
   for (int e = 0; e < 4; ++e) colm |= static_cast<uint32_t>(xs + e >= 0 && xs + e < a.W) << e;
   const bool ld = xs >= 0 && xs < a.W, whole = xs >= 0 && xs + 4 <= a.W;
   const bool out_lane = lane >= 1 && lane <= kFwLanes;
-  const bool f64 = a.out_dtype == VSR_F64;
   const T* rp = src + (ys - R) * a.pitch + xs;
   auto load = [&](int i, const T* p) -> V4 {
     const uint64_t gy = static_cast<uint64_t>(ys - R + i);
@@ -465,7 +464,180 @@ __global__ void __launch_bounds__(32 * kFwWarps) fs_warp_kernel(const FsArgs a) 
             q[c] = nd ? static_cast<float>(a.nd_out) : v;
             qd[c] = nd ? a.nd_out : static_cast<double>(v);
           }
-          if (f64) {
+          if constexpr (F64) {
+            double* op = reinterpret_cast<double*>(obase) + orow;
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+              if (xs + c < a.W) op[c] = qd[c];
+          } else {
+            float* op = reinterpret_cast<float*>(obase) + orow;
+            if (VOUT && xs + 3 < a.W) {
+              *reinterpret_cast<float4*>(op) = make_float4(q[0], q[1], q[2], q[3]);
+            } else {
+#pragma unroll
+              for (int c = 0; c < 4; ++c)
+                if (xs + c < a.W) op[c] = q[c];
+            }
+          }
+        }
+        orow += a.out_pitch;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------- register-resident std
+// 8/16-bit rasters, square windows with R <= 4, rows aligned to 4 elements.
+// Same warp strips; the statistic is shift-invariant, so values enter as
+// v' = v (int16: v + 32768 via bit 15) and the sums stay non-negative and
+// exact in 32 bits: a packed word (v' in the low bits, a count bit above,
+// as in the focal mean) and the two 16-bit halves of v'^2.  Per lane and
+// column, running vertical sums over the last 2R+1 rows: the entering row
+// added, the leaving one (kept in a register ring of raw rows) subtracted;
+// then shuffles and horizontal window sums.  n^2 var = n sum v'^2 -
+// (sum v')^2 exactly in 64 bits; a float32 output is sqrt(n^2 var)/n rounded
+// once (vsr_std_f32_small), a float64 output the FP64 form of the
+// shared-memory kernel.  A nodata centre gives the nodata value.
+template <int R, typename T, bool VOUT, bool F64>
+__global__ void __launch_bounds__(32 * kFwWarps) fs_warp_std(const FsArgs a) {
+  static_assert(R >= 1 && R <= 4, "the neighbour exchange covers radii up to 4");
+  using V4 = typename Fw4<T>::type;
+  constexpr int P = 2 * R + 1;
+  constexpr long long kTaps = static_cast<long long>(P) * P;
+  constexpr int kShift = kTaps * 65535ll < (1ll << 22) ? 22 : 23;  // value-sum bits; the count above
+  static_assert(kTaps * 65535ll < (1ll << kShift) && kTaps < (1ll << (32 - kShift)), "packed sums overflow");
+  constexpr uint32_t kOne = 1u << kShift, kLow = kOne - 1u;
+  constexpr uint32_t kFlip = std::is_signed<T>::value ? 0x8000u : 0u;
+  constexpr uint32_t kMask = sizeof(T) == 1 ? 0xFFu : 0xFFFFu;
+  const int lane = threadIdx.x & 31;
+  const int64_t xw = (static_cast<int64_t>(blockIdx.x) * kFwWarps + (threadIdx.x >> 5)) * kFwCols;
+  if (xw >= a.W) return;
+  const int64_t xs = xw - 4 + 4 * lane;
+  const int64_t ys = static_cast<int64_t>(blockIdx.y) * kFwStrip;
+  const T* src = static_cast<const T*>(a.src) + static_cast<int64_t>(blockIdx.z) * a.band_stride;
+  char* obase = static_cast<char*>(a.dst) +
+                static_cast<int64_t>(blockIdx.z) * a.out_band_stride * (F64 ? 8 : 4);
+  const int nout = static_cast<int>(a.H - ys < kFwStrip ? a.H - ys : kFwStrip);
+  const int nin = nout + 2 * R;
+  const bool has_nd = a.kind == VSR_NODATA_VALUE;
+  const uint32_t ndk = static_cast<uint32_t>(static_cast<int64_t>(a.ndv)) & kMask;
+  uint32_t colm = 0u;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) colm |= static_cast<uint32_t>(xs + e >= 0 && xs + e < a.W) << e;
+  const bool ld = xs >= 0 && xs < a.W, whole = xs >= 0 && xs + 4 <= a.W;
+  const bool out_lane = lane >= 1 && lane <= kFwLanes;
+  const T* rp = src + (ys - R) * a.pitch + xs;
+  auto load = [&](int i, const T* p) -> V4 {
+    const uint64_t gy = static_cast<uint64_t>(ys - R + i);
+    V4 v{};
+    if (ld && i < nin && gy < static_cast<uint64_t>(a.H)) {
+      if (whole) {
+        v = __ldg(reinterpret_cast<const V4*>(p));
+      } else {
+        uint32_t e[4] = {0u, 0u, 0u, 0u};
+        for (int q = 0; q < 4 && xs + q < a.W; ++q)
+          e[q] = static_cast<uint32_t>(static_cast<std::make_unsigned_t<T>>(__ldg(p + q)));
+        if constexpr (sizeof(T) == 1) v = e[0] | (e[1] << 8) | (e[2] << 16) | (e[3] << 24);
+        else v = make_uint2(e[0] | (e[1] << 16), e[2] | (e[3] << 16));
+      }
+    }
+    return v;
+  };
+  // a row's 4 elements -> packed words, v'^2 halves, validity bits
+  auto prep = [&](const V4 raw, bool rowin, uint32_t pk[4], uint32_t sh[4], uint32_t sl[4]) -> uint32_t {
+    uint32_t e4[4];
+    if constexpr (sizeof(T) == 1) {
+#pragma unroll
+      for (int e = 0; e < 4; ++e) e4[e] = (raw >> (8 * e)) & 0xFFu;
+    } else {
+      e4[0] = raw.x & 0xFFFFu;
+      e4[1] = raw.x >> 16;
+      e4[2] = raw.y & 0xFFFFu;
+      e4[3] = raw.y >> 16;
+    }
+    uint32_t m = 0u;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const bool ok = rowin && ((colm >> e) & 1u) && !(has_nd && e4[e] == ndk);
+      const uint32_t v = e4[e] ^ kFlip, sq = v * v;
+      pk[e] = ok ? (v | kOne) : 0u;
+      sh[e] = ok ? (sq >> 16) : 0u;
+      sl[e] = ok ? (sq & 0xFFFFu) : 0u;
+      m |= static_cast<uint32_t>(ok) << e;
+    }
+    return m;
+  };
+  V4 pre[P], past[P];
+#pragma unroll
+  for (int u = 0; u < P; ++u) {
+    pre[u] = load(u, rp + u * a.pitch);
+    past[u] = V4{};
+  }
+  const T* lp = rp + P * a.pitch;
+  uint32_t cs[4] = {0u, 0u, 0u, 0u}, ch[4] = {0u, 0u, 0u, 0u}, cl[4] = {0u, 0u, 0u, 0u};  // column sums
+  uint32_t vm[P];
+#pragma unroll
+  for (int u = 0; u < P; ++u) vm[u] = 0u;
+  int64_t orow = ys * a.out_pitch + xs;
+  for (int g0 = 0; g0 < nin; g0 += P) {
+#pragma unroll
+    for (int u = 0; u < P; ++u) {
+      const int i = g0 + u;
+      if (i >= nin) break;
+      const V4 rn = pre[u], ro = past[u];
+      pre[u] = load(i + P, lp);
+      lp += a.pitch;
+      past[u] = rn;
+      uint32_t pn[4], hn[4], ln[4], po[4], ho[4], lo[4];
+      vm[u] = prep(rn, static_cast<uint64_t>(ys - R + i) < static_cast<uint64_t>(a.H), pn, hn, ln);
+      prep(ro, i >= P && static_cast<uint64_t>(ys - R + i - P) < static_cast<uint64_t>(a.H), po, ho, lo);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        cs[c] += pn[c] - po[c];
+        ch[c] += hn[c] - ho[c];
+        cl[c] += ln[c] - lo[c];
+      }
+      if (i >= 2 * R) {
+        // neighbours' column sums, then the horizontal window sums
+        uint32_t ws[12], wh[12], wl[12];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          ws[4 + e] = cs[e];
+          wh[4 + e] = ch[e];
+          wl[4 + e] = cl[e];
+          ws[e] = __shfl_up_sync(0xffffffffu, cs[e], 1);
+          wh[e] = __shfl_up_sync(0xffffffffu, ch[e], 1);
+          wl[e] = __shfl_up_sync(0xffffffffu, cl[e], 1);
+          ws[8 + e] = __shfl_down_sync(0xffffffffu, cs[e], 1);
+          wh[8 + e] = __shfl_down_sync(0xffffffffu, ch[e], 1);
+          wl[8 + e] = __shfl_down_sync(0xffffffffu, cl[e], 1);
+        }
+        if (out_lane) {
+          const uint32_t cm = vm[(u + P - R) % P];  // the centre row i - R
+          uint32_t s0 = 0u, s1 = 0u, s2 = 0u;
+#pragma unroll
+          for (int j = 4 - R; j <= 4 + R; ++j) {
+            s0 += ws[j];
+            s1 += wh[j];
+            s2 += wl[j];
+          }
+          float q[4];
+          double qd[4];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            if (c > 0) {
+              s0 += ws[4 + c + R] - ws[3 + c - R];
+              s1 += wh[4 + c + R] - wh[3 + c - R];
+              s2 += wl[4 + c + R] - wl[3 + c - R];
+            }
+            const uint32_t cnt = s0 >> kShift, sum = s0 & kLow;
+            const uint64_t sq = (static_cast<uint64_t>(s1) << 16) + s2;
+            const uint64_t N = static_cast<uint64_t>(cnt) * sq - static_cast<uint64_t>(sum) * sum;  // n^2 var
+            const bool ok = (cm >> c) & 1u;  // a valid centre: cnt >= 1
+            if constexpr (F64) qd[c] = ok ? sqrt(static_cast<double>(N)) / cnt : a.nd_out;
+            else q[c] = ok ? vsr_std_f32_small(N, cnt) : static_cast<float>(a.nd_out);
+          }
+          if constexpr (F64) {
             double* op = reinterpret_cast<double*>(obase) + orow;
 #pragma unroll
             for (int c = 0; c < 4; ++c)
@@ -494,14 +666,21 @@ int fs_warp_launch(const FsArgs& a, int bands, cudaStream_t st) {
   if (grid.y > 65535u) return -1;
   const bool vout = a.out_dtype == VSR_F32 && aligned(a.dst, 16) && a.out_pitch % 4 == 0 &&
                     (bands == 1 || a.out_band_stride % 4 == 0);
-  if (vout) fs_warp_kernel<R, T, S, true><<<grid, 32 * kFwWarps, 0, st>>>(a);
-  else fs_warp_kernel<R, T, S, false><<<grid, 32 * kFwWarps, 0, st>>>(a);
+  if constexpr (S == VSR_STAT_STD) {
+    if (a.out_dtype == VSR_F64) fs_warp_std<R, T, false, true><<<grid, 32 * kFwWarps, 0, st>>>(a);
+    else if (vout) fs_warp_std<R, T, true, false><<<grid, 32 * kFwWarps, 0, st>>>(a);
+    else fs_warp_std<R, T, false, false><<<grid, 32 * kFwWarps, 0, st>>>(a);
+  } else {
+    if (a.out_dtype == VSR_F64) fs_warp_kernel<R, T, S, false, true><<<grid, 32 * kFwWarps, 0, st>>>(a);
+    else if (vout) fs_warp_kernel<R, T, S, true, false><<<grid, 32 * kFwWarps, 0, st>>>(a);
+    else fs_warp_kernel<R, T, S, false, false><<<grid, 32 * kFwWarps, 0, st>>>(a);
+  }
   VSR_CUDA_TRY(cudaGetLastError());
   return VSR_OK;
 }
 
-// The register-resident form when it applies (8/16-bit min / max / range,
-// square window of radius 1..4, rows aligned to 4 elements); -1 otherwise.
+// The register-resident form when it applies (8/16-bit min / max / range /
+// std, square window of radius 1..4, rows aligned to 4 elements); -1 otherwise.
 template <typename T, int S>
 int fs_warp_try(const FsArgs& a, int bands, cudaStream_t st) {
   if (a.ry != a.rx || a.ry < 1 || a.ry > 4) return -1;
@@ -531,6 +710,14 @@ int fs_launch(const FsArgs& a, int bands, cudaStream_t st) {
 template <int S>
 int fs_dispatch(const FsArgs& a, int bands, cudaStream_t st) {
   if constexpr (S == VSR_STAT_STD) {
+    int rc = -1;
+    switch (a.dtype) {
+      case VSR_U8: rc = fs_warp_try<uint8_t, S>(a, bands, st); break;
+      case VSR_I16: rc = fs_warp_try<int16_t, S>(a, bands, st); break;
+      case VSR_U16: rc = fs_warp_try<uint16_t, S>(a, bands, st); break;
+      default: break;
+    }
+    if (rc >= 0) return rc;
     switch (a.dtype) {
       case VSR_U8: return fs_launch<uint8_t, int32_t, S>(a, bands, st);
       case VSR_I16: return fs_launch<int16_t, int32_t, S>(a, bands, st);

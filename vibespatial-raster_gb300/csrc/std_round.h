@@ -78,4 +78,38 @@ VSR_SR_FN float vsr_std_f32(uint64_t N, uint32_t n) {
   return y;
 }
 
+// The same for windows of at most 127 taps (n < 2^7): every (a n) with
+// a < 2^25 is below 2^32, so its square fits one 64-bit word and a midpoint
+// test is a shift and a 64-bit compare.
+VSR_SR_FN int vsr_sr_cmp_small(uint64_t N, uint32_t n, uint64_t a, int b) {
+  const int s = -2 * b;  // > 0
+  const uint64_t p = a * n, pp = p * p;
+  if (s >= 64 || (N >> (64 - s)) != 0) return N ? 1 : -1;  // N 2^s >= 2^64 > pp (N > 0 here)
+  const uint64_t ns = N << s;
+  return ns > pp ? 1 : (ns < pp ? -1 : 0);
+}
+
+VSR_SR_FN float vsr_std_f32_small(uint64_t N, uint32_t n) {
+  if (N == 0) return 0.0f;
+  float y = sqrtf((float)N) / (float)n;
+  for (int it = 0; it < 6; ++it) {
+    const uint32_t u = vsr_sr_bits(y);
+    const int ex = (int)((u >> 23) & 0xffu) - 150;
+    const uint64_t m = (u & 0x7fffffu) | 0x800000u;
+    const int up = vsr_sr_cmp_small(N, n, 2 * m + 1, ex - 1);
+    if (up > 0 || (up == 0 && (m & 1u))) {
+      y = vsr_sr_float(u + 1u);
+      continue;
+    }
+    const int lo = m > 0x800000u ? vsr_sr_cmp_small(N, n, 2 * m - 1, ex - 1)
+                                 : vsr_sr_cmp_small(N, n, 4 * m - 1, ex - 2);
+    if (lo < 0 || (lo == 0 && (m & 1u))) {
+      y = vsr_sr_float(u - 1u);
+      continue;
+    }
+    break;
+  }
+  return y;
+}
+
 #endif
