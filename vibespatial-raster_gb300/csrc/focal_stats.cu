@@ -493,8 +493,8 @@ __global__ void __launch_bounds__(32 * kFwWarps) fs_warp_kernel(const FsArgs a) 
 // exact in 32 bits: a packed word (v' in the low bits, a count bit above,
 // as in the focal mean) and the two 16-bit halves of v'^2.  Per lane and
 // column, running vertical sums over the last 2R+1 rows: the entering row
-// added, the leaving one (kept in a register ring of raw rows) subtracted;
-// then shuffles and horizontal window sums.  n^2 var = n sum v'^2 -
+// added, the leaving one (kept in a shared-memory ring of raw rows, one slot
+// column per thread) subtracted; then shuffles and horizontal window sums.  n^2 var = n sum v'^2 -
 // (sum v')^2 exactly in 64 bits; a float32 output is sqrt(n^2 var)/n rounded
 // once (vsr_std_f32_small), a float64 output the FP64 form of the
 // shared-memory kernel.  A nodata centre gives the nodata value.
@@ -567,95 +567,96 @@ __global__ void __launch_bounds__(32 * kFwWarps) fs_warp_std(const FsArgs a) {
     }
     return m;
   };
-  V4 pre[P], past[P];
+  // the window's raw rows in a shared-memory ring, one slot column per
+  // thread (each thread reads only its own slots: no barrier); the row loop
+  // is not unrolled, so the long output code exists once
+  __shared__ V4 ring[P][32 * kFwWarps];
+  const int t = threadIdx.x;
 #pragma unroll
-  for (int u = 0; u < P; ++u) {
-    pre[u] = load(u, rp + u * a.pitch);
-    past[u] = V4{};
-  }
-  const T* lp = rp + P * a.pitch;
+  for (int u = 0; u < P; ++u) ring[u][t] = V4{};
+  V4 nxt = load(0, rp);  // one row ahead
+  const T* lp = rp + a.pitch;
   uint32_t cs[4] = {0u, 0u, 0u, 0u}, ch[4] = {0u, 0u, 0u, 0u}, cl[4] = {0u, 0u, 0u, 0u};  // column sums
-  uint32_t vm[P];
-#pragma unroll
-  for (int u = 0; u < P; ++u) vm[u] = 0u;
   int64_t orow = ys * a.out_pitch + xs;
-  for (int g0 = 0; g0 < nin; g0 += P) {
+  int slot = 0, cslot = P - R;  // ring slots of rows i and i - R
+#pragma unroll 1
+  for (int i = 0; i < nin; ++i) {
+    const V4 rn = nxt;
+    nxt = load(i + 1, lp);
+    lp += a.pitch;
+    const V4 ro = ring[slot][t];  // row i - P, leaving the window
+    ring[slot][t] = rn;
+    uint32_t pn[4], hn[4], ln[4], po[4], ho[4], lo[4];
+    prep(rn, static_cast<uint64_t>(ys - R + i) < static_cast<uint64_t>(a.H), pn, hn, ln);
+    prep(ro, i >= P && static_cast<uint64_t>(ys - R + i - P) < static_cast<uint64_t>(a.H), po, ho, lo);
 #pragma unroll
-    for (int u = 0; u < P; ++u) {
-      const int i = g0 + u;
-      if (i >= nin) break;
-      const V4 rn = pre[u], ro = past[u];
-      pre[u] = load(i + P, lp);
-      lp += a.pitch;
-      past[u] = rn;
-      uint32_t pn[4], hn[4], ln[4], po[4], ho[4], lo[4];
-      vm[u] = prep(rn, static_cast<uint64_t>(ys - R + i) < static_cast<uint64_t>(a.H), pn, hn, ln);
-      prep(ro, i >= P && static_cast<uint64_t>(ys - R + i - P) < static_cast<uint64_t>(a.H), po, ho, lo);
+    for (int c = 0; c < 4; ++c) {
+      cs[c] += pn[c] - po[c];
+      ch[c] += hn[c] - ho[c];
+      cl[c] += ln[c] - lo[c];
+    }
+    if (i >= 2 * R) {
+      // neighbours' column sums, then the horizontal window sums
+      uint32_t ws[12], wh[12], wl[12];
 #pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        cs[c] += pn[c] - po[c];
-        ch[c] += hn[c] - ho[c];
-        cl[c] += ln[c] - lo[c];
+      for (int e = 0; e < 4; ++e) {
+        ws[4 + e] = cs[e];
+        wh[4 + e] = ch[e];
+        wl[4 + e] = cl[e];
+        ws[e] = __shfl_up_sync(0xffffffffu, cs[e], 1);
+        wh[e] = __shfl_up_sync(0xffffffffu, ch[e], 1);
+        wl[e] = __shfl_up_sync(0xffffffffu, cl[e], 1);
+        ws[8 + e] = __shfl_down_sync(0xffffffffu, cs[e], 1);
+        wh[8 + e] = __shfl_down_sync(0xffffffffu, ch[e], 1);
+        wl[8 + e] = __shfl_down_sync(0xffffffffu, cl[e], 1);
       }
-      if (i >= 2 * R) {
-        // neighbours' column sums, then the horizontal window sums
-        uint32_t ws[12], wh[12], wl[12];
+      if (out_lane) {
+        // the centre row i - R (inside the raster: an output row)
+        uint32_t pc[4], hc[4], lc[4];
+        const uint32_t cm = prep(ring[cslot][t], true, pc, hc, lc);
+        uint32_t s0 = 0u, s1 = 0u, s2 = 0u;
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          ws[4 + e] = cs[e];
-          wh[4 + e] = ch[e];
-          wl[4 + e] = cl[e];
-          ws[e] = __shfl_up_sync(0xffffffffu, cs[e], 1);
-          wh[e] = __shfl_up_sync(0xffffffffu, ch[e], 1);
-          wl[e] = __shfl_up_sync(0xffffffffu, cl[e], 1);
-          ws[8 + e] = __shfl_down_sync(0xffffffffu, cs[e], 1);
-          wh[8 + e] = __shfl_down_sync(0xffffffffu, ch[e], 1);
-          wl[8 + e] = __shfl_down_sync(0xffffffffu, cl[e], 1);
+        for (int j = 4 - R; j <= 4 + R; ++j) {
+          s0 += ws[j];
+          s1 += wh[j];
+          s2 += wl[j];
         }
-        if (out_lane) {
-          const uint32_t cm = vm[(u + P - R) % P];  // the centre row i - R
-          uint32_t s0 = 0u, s1 = 0u, s2 = 0u;
+        float q[4];
+        double qd[4];
 #pragma unroll
-          for (int j = 4 - R; j <= 4 + R; ++j) {
-            s0 += ws[j];
-            s1 += wh[j];
-            s2 += wl[j];
+        for (int c = 0; c < 4; ++c) {
+          if (c > 0) {
+            s0 += ws[4 + c + R] - ws[3 + c - R];
+            s1 += wh[4 + c + R] - wh[3 + c - R];
+            s2 += wl[4 + c + R] - wl[3 + c - R];
           }
-          float q[4];
-          double qd[4];
+          const uint32_t cnt = s0 >> kShift, sum = s0 & kLow;
+          const uint64_t sq = (static_cast<uint64_t>(s1) << 16) + s2;
+          const uint64_t N = static_cast<uint64_t>(cnt) * sq - static_cast<uint64_t>(sum) * sum;  // n^2 var
+          const bool ok = (cm >> c) & 1u;  // a valid centre: cnt >= 1
+          if constexpr (F64) qd[c] = ok ? sqrt(static_cast<double>(N)) / cnt : a.nd_out;
+          else q[c] = ok ? vsr_std_f32_small(N, cnt) : static_cast<float>(a.nd_out);
+        }
+        if constexpr (F64) {
+          double* op = reinterpret_cast<double*>(obase) + orow;
 #pragma unroll
-          for (int c = 0; c < 4; ++c) {
-            if (c > 0) {
-              s0 += ws[4 + c + R] - ws[3 + c - R];
-              s1 += wh[4 + c + R] - wh[3 + c - R];
-              s2 += wl[4 + c + R] - wl[3 + c - R];
-            }
-            const uint32_t cnt = s0 >> kShift, sum = s0 & kLow;
-            const uint64_t sq = (static_cast<uint64_t>(s1) << 16) + s2;
-            const uint64_t N = static_cast<uint64_t>(cnt) * sq - static_cast<uint64_t>(sum) * sum;  // n^2 var
-            const bool ok = (cm >> c) & 1u;  // a valid centre: cnt >= 1
-            if constexpr (F64) qd[c] = ok ? sqrt(static_cast<double>(N)) / cnt : a.nd_out;
-            else q[c] = ok ? vsr_std_f32_small(N, cnt) : static_cast<float>(a.nd_out);
-          }
-          if constexpr (F64) {
-            double* op = reinterpret_cast<double*>(obase) + orow;
+          for (int c = 0; c < 4; ++c)
+            if (xs + c < a.W) op[c] = qd[c];
+        } else {
+          float* op = reinterpret_cast<float*>(obase) + orow;
+          if (VOUT && xs + 3 < a.W) {
+            *reinterpret_cast<float4*>(op) = make_float4(q[0], q[1], q[2], q[3]);
+          } else {
 #pragma unroll
             for (int c = 0; c < 4; ++c)
-              if (xs + c < a.W) op[c] = qd[c];
-          } else {
-            float* op = reinterpret_cast<float*>(obase) + orow;
-            if (VOUT && xs + 3 < a.W) {
-              *reinterpret_cast<float4*>(op) = make_float4(q[0], q[1], q[2], q[3]);
-            } else {
-#pragma unroll
-              for (int c = 0; c < 4; ++c)
-                if (xs + c < a.W) op[c] = q[c];
-            }
+              if (xs + c < a.W) op[c] = q[c];
           }
         }
-        orow += a.out_pitch;
       }
+      orow += a.out_pitch;
     }
+    slot = slot + 1 == P ? 0 : slot + 1;
+    cslot = cslot + 1 == P ? 0 : cslot + 1;
   }
 }
 

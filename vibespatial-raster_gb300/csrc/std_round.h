@@ -91,25 +91,25 @@ VSR_SR_FN int vsr_sr_cmp_small(uint64_t N, uint32_t n, uint64_t a, int b) {
 
 VSR_SR_FN float vsr_std_f32_small(uint64_t N, uint32_t n) {
   if (N == 0) return 0.0f;
-  float y = sqrtf((float)N) / (float)n;
-  for (int it = 0; it < 6; ++it) {
-    const uint32_t u = vsr_sr_bits(y);
-    const int ex = (int)((u >> 23) & 0xffu) - 150;
-    const uint64_t m = (u & 0x7fffffu) | 0x800000u;
-    const int up = vsr_sr_cmp_small(N, n, 2 * m + 1, ex - 1);
-    if (up > 0 || (up == 0 && (m & 1u))) {
-      y = vsr_sr_float(u + 1u);
-      continue;
-    }
-    const int lo = m > 0x800000u ? vsr_sr_cmp_small(N, n, 2 * m - 1, ex - 1)
-                                 : vsr_sr_cmp_small(N, n, 4 * m - 1, ex - 2);
-    if (lo < 0 || (lo == 0 && (m & 1u))) {
-      y = vsr_sr_float(u - 1u);
-      continue;
-    }
-    break;
+  // estimate within two ulps: N through two 32-bit halves (no 64-bit
+  // conversion), correctly rounded sqrt and division
+  const float nf = (float)(uint32_t)(N >> 32) * 4294967296.0f + (float)(uint32_t)N;
+  const uint32_t u = vsr_sr_bits(sqrtf(nf) / (float)n);
+  // the result is u - 2 .. u + 2: count the midpoints between consecutive
+  // candidates that lie below sqrt(N)/n (a tie goes to the even candidate);
+  // the midpoint above float ud is (2 m + 1) 2^(ex - 1) for ud = m 2^ex,
+  // across a binade boundary too.  No branch: every lane runs the same four
+  // tests.
+  int k = -2;
+#pragma unroll
+  for (int d = -2; d < 2; ++d) {
+    const uint32_t ud = u + (uint32_t)d;
+    const int ex = (int)((ud >> 23) & 0xffu) - 150;
+    const uint64_t m = (ud & 0x7fffffu) | 0x800000u;
+    const int c = vsr_sr_cmp_small(N, n, 2 * m + 1, ex - 1);
+    k += (c > 0 || (c == 0 && (ud & 1u))) ? 1 : 0;
   }
-  return y;
+  return vsr_sr_float(u + (uint32_t)k);
 }
 
 #endif

@@ -10,6 +10,7 @@ It is the small, single-kernel command to run under a profiler:
                 (the 8192^2 convolution workload at a chosen size)
     focal_mean  uint16 band stack, gamma-like values 0..9999, 3 % nodata 0
                 (the 12 x 10980^2 multiband workload, fewer bands)
+    focal_stat  the same stack, one focal statistic (--stat), float32 output
     gaussian    the same uint16 stack, Gaussian sigma / kernel size
                 (--precision split_bf16: the tensor-core line passes;
                 fp32: the separable CUDA-core kernels)
@@ -60,7 +61,9 @@ def _uint16_stack(bands: int, size: int):
 
 def main(argv=None) -> None:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
-    ap.add_argument("op", choices=["conv", "focal_mean", "gaussian", "horn", "batch"])
+    ap.add_argument("op", choices=["conv", "focal_mean", "focal_stat", "gaussian", "horn", "batch"])
+    ap.add_argument("--stat", default="std", choices=["min", "max", "std", "range", "variety"],
+                    help="focal_stat: the statistic")
     ap.add_argument("--size", type=int, default=None, help="raster side (default: 4096 conv, 10980 others)")
     ap.add_argument("--bands", type=int, default=1)
     ap.add_argument("--k", type=int, default=31, help="kernel side (conv, gaussian)")
@@ -121,6 +124,9 @@ def main(argv=None) -> None:
         out = torch.empty((args.bands, n, n), dtype=torch.float32, device=dev)
         if args.op == "focal_mean":
             fn = lambda: algebra.focal_mean_bands(r, args.radius, args.radius, out_dtype=np.float32, out=out)  # noqa: E731
+        elif args.op == "focal_stat":
+            fn = lambda: algebra.focal_stat_bands(r, args.stat, args.radius, args.radius,  # noqa: E731
+                                                  out_dtype=np.float32, out=out)
         else:
             fn = lambda: algebra.gaussian_bands(r, args.sigma, args.k, precision=args.precision,  # noqa: E731
                                                 out_dtype=np.float32, out=out)
