@@ -962,7 +962,7 @@ def leg_decode(args, dev, gpu) -> dict:
         "e2e": {"value": px / e2e_s / 1e9, "unit": UNIT, "ms_per_call": e2e_s * 1e3, "h2d_bytes_per_call": size},
         "l2": "268 MB in place + 268 MB out per call exceed L2; no flush",
         "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                     "peak_source": src, "kernel": "tiff_assemble_kernel (one thread per tile row)",
+                     "peak_source": src, "kernel": "tiff_assemble_kernel (one warp per chunk row)",
                      "bytes_per_px": 12},
         "cpu_baseline": {"value": 1.0 / cpu_s / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
                          "sample": "16 tiles inflated (zlib) + 4 tiles' byte planes undone (numpy), per-pixel "

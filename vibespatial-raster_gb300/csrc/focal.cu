@@ -1021,7 +1021,8 @@ int launch_box_fast(const BoxArgs& a, cudaStream_t st, int bands) {
 
 // ------------------------------------------------------- box_slide_int --
 // Focal mean of 8/16-bit integer rasters with a square (2R+1)^2 window,
-// R <= 7: the C5 multiband workload (12 x 10980^2 uint16, 7 x 7).
+// R <= 7, rows of any alignment (box_warp_int, below, takes R <= 4 with rows
+// aligned to 4 elements, e.g. the 12 x 10980^2 uint16 stack's 7 x 7 mean).
 //
 // Each tap is packed into one 32-bit word, value (offset to be
 // non-negative) in the low bits and a count bit above them:
