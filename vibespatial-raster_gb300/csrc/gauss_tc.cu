@@ -245,15 +245,16 @@ __device__ __forceinline__ uint32_t hadd2_bits(uint32_t a, uint32_t b) {
 }
 
 // 8 values as one 16-byte row of F16 hi parts and one of lo parts, element
-// order reversed (element 0 holds v[7]).
+// order reversed (element 0 holds v[7]); the residuals in packed f32x2
+// (rounded as the scalar subtraction).
 __device__ __forceinline__ void split_row8(const float v[8], uint4& hi, uint4& lo) {
   uint32_t h[4], l[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    const float a = v[7 - 2 * q], b = v[6 - 2 * q];
-    const __half2 hv = __floats2half2_rn(a, b);
-    const float2 hf = __half22float2(hv);
-    const __half2 lv = __floats2half2_rn(a - hf.x, b - hf.y);
+    const float2 ab = make_float2(v[7 - 2 * q], v[6 - 2 * q]);
+    const __half2 hv = __floats2half2_rn(ab.x, ab.y);
+    const float2 r = __ffma2_rn(__half22float2(hv), make_float2(-1.0f, -1.0f), ab);
+    const __half2 lv = __floats2half2_rn(r.x, r.y);
     h[q] = f16x2_bits(hv);
     l[q] = f16x2_bits(lv);
   }
@@ -528,10 +529,18 @@ __global__ void __launch_bounds__(kRThreads, 1) gauss_row_kernel(const GaussArgs
           if (!store || y0 >= h8) continue;
           float num[8], den[8];
 #pragma unroll
-          for (int e = 0; e < 8; ++e) {
+          for (int e = 0; e < 8; e += 2) {  // packed pairs: (256 D_h + D_l) 2^-13, D_v 2^-4
             const int n = 8 * c2 + e;
-            num[e] = fmaf(__uint_as_float(rh[n]), 0.03125f, __uint_as_float(rl[n]) * 0.0001220703125f);
-            den[e] = __uint_as_float(rv[n]) * 0.0625f;
+            const float2 nl = __fmul2_rn(make_float2(__uint_as_float(rl[n]), __uint_as_float(rl[n + 1])),
+                                         make_float2(0.0001220703125f, 0.0001220703125f));
+            const float2 nn = __ffma2_rn(make_float2(__uint_as_float(rh[n]), __uint_as_float(rh[n + 1])),
+                                         make_float2(0.03125f, 0.03125f), nl);
+            const float2 dd = __fmul2_rn(make_float2(__uint_as_float(rv[n]), __uint_as_float(rv[n + 1])),
+                                         make_float2(0.0625f, 0.0625f));
+            num[e] = nn.x;
+            num[e + 1] = nn.y;
+            den[e] = dd.x;
+            den[e + 1] = dd.y;
           }
           if (!xin || y0 + 8 > a.lines) {  // rows past the raster, or a column past it: zeros
             const int nrow = xin ? static_cast<int>(a.lines - y0) : 0;
