@@ -308,8 +308,9 @@ VSR_API int vsr_focal_mean_bands(const void* src, int dtype, int bands, int64_t 
  *   VSR_STAT_MEAN        as vsr_focal_mean;
  *   VSR_STAT_STD         population standard deviation of the valid
  *                        (non-nodata, non-NaN) taps, 0.0 for an empty window;
- *                        exact integer sums for 8/16-bit rasters, two passes
- *                        in float64 otherwise;
+ *                        exact integer sums for 8/16-bit rasters (a VSR_F32
+ *                        output is sqrt(n^2 var)/n rounded once to float32),
+ *                        two passes in float64 otherwise;
  *   VSR_STAT_RANGE       max - min of the valid taps;
  *   VSR_STAT_VARIETY     number of distinct valid values, 0 for an empty
  *                        window (no cap; the reference GPU kernel stops at 49).
