@@ -10,6 +10,11 @@
   tests, no FP64); compared with a long-double reference over random and
   edge-case (N, n), perfect squares included.
 
+* csrc/terrain_exact.h: TRI and TPI of float32 windows whose values share a
+  narrow binade range as exact integers, written as float64 bits; compared
+  bit for bit with the reference's float64 formulas on random DEM-like,
+  negative and tiny windows.
+
 The GPU side is covered by the derivative and focal-statistics parity tests.
 """
 
@@ -43,3 +48,9 @@ def test_f32_widen_matches_conversion(tmp_path):
 def test_std_f32_is_correctly_rounded(tmp_path):
     *_, n, bad = _run(tmp_path, "std_round_check.c", "2000000")
     assert n == 2000000 and bad == 0
+
+
+def test_exact_tri_tpi_match_float64(tmp_path):
+    n, accepted, bad = _run(tmp_path, "terrain_exact_check.c", "2000000")
+    assert bad == 0
+    assert accepted > n // 2  # DEM-like windows take the integer path

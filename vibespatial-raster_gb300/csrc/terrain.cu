@@ -27,6 +27,7 @@
 
 #include "vsr_internal.cuh"
 #include "df_round.h"
+#include "terrain_exact.h"
 
 namespace vsr {
 namespace {
@@ -101,6 +102,14 @@ __device__ __forceinline__ double df_to_double(float hi, float lo) {
          __hiloint2double(static_cast<int>(lh), static_cast<int>(ll));
 }
 
+// s 2^e (exact, |s| < 2^31) as the output: float64 bits written directly,
+// float32 rounded once.
+__device__ __forceinline__ void store_int_scaled(void* base, int out_dtype, int64_t i, int32_t s, int e) {
+  const double v = __longlong_as_double(static_cast<long long>(vsr_int_scaled_bits(s, e)));
+  if (out_dtype == VSR_F64) static_cast<double*>(base)[i] = v;
+  else static_cast<float*>(base)[i] = static_cast<float>(v);
+}
+
 __device__ __forceinline__ void store_df(void* base, int out_dtype, int64_t i, DF v) {
   if (out_dtype == VSR_F64) static_cast<double*>(base)[i] = df_to_double(v.hi, v.lo);
   else static_cast<float*>(base)[i] = v.hi + v.lo;
@@ -173,6 +182,31 @@ __global__ void __launch_bounds__(kDTW * kDTH) terrain_deriv_kernel(const T* __r
   f9 = f5 && fabs(z[0]) <= static_cast<C>(3.4e38) && fabs(z[2]) <= static_cast<C>(3.4e38) &&
        fabs(z[6]) <= static_cast<C>(3.4e38) && fabs(z[8]) <= static_cast<C>(3.4e38);
   if (kDF) {
+    // TRI and TPI as exact integers when the window's values share a narrow
+    // binade range (terrain_exact.h): the reference's float64 results bit for
+    // bit, no double-float arithmetic
+    uint32_t bits[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) bits[k] = __float_as_uint(static_cast<float>(z[k]));
+    int32_t t8 = 0, p8 = 0;
+    int e2 = 0;
+    if ((P.tri || P.tpi) && vsr_tt_exact(bits, &t8, &p8, &e2)) {
+      if (P.tri) store_int_scaled(P.tri, P.out_dtype, o, t8, e2 - 3);
+      if (P.tpi) store_int_scaled(P.tpi, P.out_dtype, o, p8, e2 - 3);
+      if (P.curv) {
+        if (f5) {
+          const float z4 = static_cast<float>(z[4]);
+          const DF dw = two_diff_df(static_cast<float>(z[3]), z4), de = two_diff_df(static_cast<float>(z[5]), z4);
+          const DF dn = two_diff_df(static_cast<float>(z[1]), z4), ds = two_diff_df(static_cast<float>(z[7]), z4);
+          const DF dx = df_scale(df_add(dw, de), 0.5f), dy = df_scale(df_add(dn, ds), 0.5f);
+          const DF e = df_add(df_mul(dx, DF{P.icx2_hi, P.icx2_lo}), df_mul(dy, DF{P.icy2_hi, P.icy2_lo}));
+          store_df(P.curv, P.out_dtype, o, df_mul_f(e, -200.0f));
+        } else {
+          store_out(P.curv, P.out_dtype, o, plain_curv(z, P));
+        }
+      }
+      return;
+    }
     // error-free neighbour differences d_i = z_i - z4 (i = 0..3, 5..8)
     DF d[8];
 #pragma unroll
